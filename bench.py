@@ -1,0 +1,344 @@
+"""Benchmark: Lloyd k-means iteration throughput on GB300 (points*iterations/s).
+
+Workload (default): n = 2^28 points, d = 4 features, k = 16 clusters, float32,
+column-major, from a 16-blob Gaussian mixture (centres U[-10,10]^4, sigma
+U[0.5,2]), generated on the device from seed 42; initial centroids = first k
+points.  One step = one Lloyd iteration over all points = ONE launch of the
+fused kernel (label + mass + feature sums + FP64 merge + divide).
+
+JSON line keys (rank 0):
+  value      pts*it/s with the points resident in HBM (4 GiB > L2, so no L2
+             flush is needed between steps)
+  e2e        the same metric through the C ABI ckm_kmeans_run_f32 (the
+             AbstractKmeans::operator() call) with pinned HOST buffers: every
+             step copies the points in, runs the configured 50 iterations and
+             copies centroids, labels and masses out
+  roofline   HBM roofline of the fused kernel: algorithmic bytes per point-
+             iteration = 4*d (points read once) + 4 (label written)
+  cpu_baseline  the oracle (a restatement of the reference's single-threaded
+             KmeansNaive) on a 2^22-point sample of the same workload
+
+--impl reference runs the reference's CPU path (the oracle port, threaded
+over all host cores) on a bounded sample instead.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (n, d, k, blobs, sigma_lo, sigma_hi, iterations of the configured run)
+    "lloyd_n2^28_d4_k16": (1 << 28, 4, 16, 16, 0.5, 2.0, 50),
+    "lloyd_n2^20_d4_k10": (1 << 20, 4, 10, 10, 1.0, 1.0, 30),
+}
+DEFAULT_WORKLOAD = "lloyd_n2^28_d4_k16"
+SEED = 42
+FALLBACK_HBM_GBS = 6800.0
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                j = json.load(f)
+            for key in ("hbm_gbs", "hbm_GBps", "hbm_copy_gbs"):
+                if key in j and j[key]:
+                    return float(j[key]), "measured"
+        except (OSError, ValueError):
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic_per_point(workload):
+    """DRAM bytes per point-iteration from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "fused_lowd_d4_k16.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.strip().startswith("dram_bytes_per_point:"):
+                try:
+                    return float(line.split(":", 1)[1].strip())
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_port_rate(P, n, d, k, iters, threads):
+    """pts*it/s of the oracle's Lloyd on the given sample (wall clock)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    C0 = O.first_x_f32(P, n, d, k)
+    t0 = time.perf_counter()
+    if threads <= 1:
+        O.lloyd_f32(P, n, d, k, iters, C0)
+    else:
+        O.lloyd_f32_mt(P, n, d, k, iters, C0, threads)
+    dt = time.perf_counter() - t0
+    return n * iters / dt, dt
+
+
+def host_sample(n_s, d, blobs, slo, shi):
+    """A host-generated sample with the workload's distribution (numpy, same
+    mixture parameters and seed), so the CPU arm touches no GPU code."""
+    rng = np.random.default_rng(SEED)
+    centres = rng.uniform(-10.0, 10.0, size=(blobs, d))
+    sig = rng.uniform(slo, shi, size=blobs)
+    comp = rng.integers(0, blobs, size=n_s)
+    X = centres[comp] + sig[comp, None] * rng.standard_normal((n_s, d))
+    return np.ascontiguousarray(X.astype(np.float32).T).reshape(-1)
+
+
+def run_reference_arm(args, workload):
+    n, d, k, blobs, slo, shi, iters_cfg = WORKLOADS[workload]
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    # bounded sample of the workload, sized from a probe so the whole
+    # warmup + steps run stays within a couple of minutes
+    probe_n = 1 << 18
+    P = host_sample(1 << 22, d, blobs, slo, shi)
+    Pp = np.ascontiguousarray(P.reshape(d, -1)[:, :probe_n]).reshape(-1)
+    rate, _ = cpu_port_rate(Pp, probe_n, d, k, 2, threads)
+    budget_s = 90.0
+    per_step_pts = max(1 << 14, min(1 << 22, int(rate * budget_s / max(1, args.steps + args.warmup))))
+    n_s = 1 << int(np.floor(np.log2(per_step_pts)))
+    Ps = np.ascontiguousarray(P.reshape(d, -1)[:, :n_s]).reshape(-1)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    C = O.first_x_f32(Ps, n_s, d, k)
+    for _ in range(args.warmup):
+        C, _, _ = O.lloyd_f32_mt(Ps, n_s, d, k, 1, C, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        C, _, _ = O.lloyd_f32_mt(Ps, n_s, d, k, 1, C, threads)
+    dt = time.perf_counter() - t0
+    value = n_s * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "pts*iter/s", "value": value, "unit": "pts*iter/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Gaussian mixture, sample of the workload)",
+        "config": {"workload": workload, "n": n, "d": d, "k": k, "sample_points": n_s,
+                   "implementation": "oracle port of the reference KmeansNaive (kmeans_naive.cpp), "
+                                     "labeling split over host threads"},
+        "cpu_baseline": {"value": value, "unit": "pts*iter/s", "cores": threads, "kind": "port",
+                         "sample": "%d points of the workload, 1 iteration per step" % n_s},
+        "e2e": {"value": value, "unit": "pts*iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    workload = args.workload
+
+    if args.impl == "reference":
+        return run_reference_arm(args, workload)
+
+    import importlib
+
+    import torch
+
+    rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    ckm = importlib.import_module("cl-kmeans_gb300")
+    ckm.lib()
+    n, d, k, blobs, slo, shi, iters_cfg = WORKLOADS[workload]
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+
+    # --- inputs resident in HBM (generated on the device) ---------------------
+    P = torch.empty(n * d, dtype=torch.float32, device=dev)
+    ckm.generate_mixture(P, n, d, blobs, SEED + rank, sigma=(slo, shi))
+    C = [torch.empty(k * d, dtype=torch.float32, device=dev) for _ in range(2)]
+    C[0].copy_(P.view(d, n)[:, :k].reshape(-1))   # first_x: C[f*k+c] = P[f*n+c]
+    C0_host = C[0].cpu().numpy().copy()
+    L = torch.empty(n, dtype=torch.int32, device=dev)
+    M = torch.empty(k, dtype=torch.int32, device=dev)
+    S = ckm.new_scratch(d, k, dev)
+    torch.cuda.synchronize()
+
+    def step(i):
+        ckm.fused(P, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = ckm.launch_count()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        step(args.warmup + i)
+        evs[i][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    gpu_launches = ckm.launch_count() - launches0
+    clocks = sampler.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    per_launch_ms = [a.elapsed_time(b) for a, b in evs]
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = n * args.steps * world / (total_ms / 1e3)
+    avg_launch_s = statistics.mean(per_launch_ms) / 1e3
+
+    # --- roofline of the fused kernel --------------------------------------
+    bytes_per_point = 4 * d + 4
+    achieved = bytes_per_point * n / avg_launch_s / 1e9
+    peak, peak_kind = measured_hbm_peak()
+    tpp = profiled_traffic_per_point(workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind,
+                "traffic": (tpp * n) if tpp is not None else None,
+                "algorithmic_bytes_per_launch": bytes_per_point * n}
+
+    # --- e2e through the C ABI with pinned host buffers --------------------
+    e2e = None
+    if True:
+        hostP = torch.empty(n * d, dtype=torch.float32, pin_memory=True)
+        hostP.copy_(P)
+        hp = hostP.numpy()
+        hostC = torch.empty(k * d, dtype=torch.float32, pin_memory=True)
+        hostL = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        hostM = torch.empty(k, dtype=torch.int32, pin_memory=True)
+        cfg = ckm.RunConfig(b"single_stage", b"feature_sum", b"unroll_vector", b"part_local", b"feature_sum",
+                            local, 0, 0)
+        info = ckm.RunInfo()
+        times = []
+        for _ in range(args.e2e_steps + 1):
+            hostC.numpy()[:] = C0_host
+            t0 = time.perf_counter()
+            ckm.check(ckm.lib().ckm_kmeans_run_f32(ctypes.byref(cfg), iters_cfg, d, n, k, hp.ctypes.data,
+                                                   hostC.data_ptr(), hostM.data_ptr(), hostL.data_ptr(),
+                                                   ctypes.byref(info)), "ckm_kmeans_run_f32")
+            times.append(time.perf_counter() - t0)
+        e2e_t = statistics.mean(times[1:])
+        e2e = {"value": n * iters_cfg / e2e_t, "unit": "pts*iter/s",
+               "h2d_bytes_per_step": int(info.h2d_bytes), "d2h_bytes_per_step": int(info.d2h_bytes),
+               "iterations_per_step": iters_cfg, "ms_per_step": e2e_t * 1e3,
+               "total_time_window_ms": info.total_time_ns / 1e6}
+        del hostP
+
+    # --- CPU baseline (oracle port, single thread, bounded sample) ---------
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n_s, it_s = 1 << 22, iters_cfg
+        Ps = np.ascontiguousarray(P.view(d, n)[:, :n_s].cpu().numpy()).reshape(-1)
+        rate, dt = cpu_port_rate(Ps, n_s, d, k, it_s, 1)
+        cpu = {"value": rate, "unit": "pts*iter/s", "cores": 1, "kind": "port",
+               "sample": "first %d points of the workload, %d iterations, %.1f s" % (n_s, it_s, dt)}
+
+    if rank == 0:
+        line = {
+            "metric": "pts*iter/s", "value": value, "unit": "pts*iter/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian mixture generated on the device)",
+            "config": {"workload": workload, "n": n, "d": d, "k": k, "blobs": blobs, "sigma": [slo, shi],
+                       "seed": SEED, "init": "first_x", "layout": "column-major",
+                       "l2": "inputs (%.1f GiB) larger than L2, no flush" % (n * (d + 1) * 4 / 2 ** 30),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(gpu_launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

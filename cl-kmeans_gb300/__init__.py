@@ -1,0 +1,248 @@
+"""GB300-native Lloyd k-means: Python handle on libckm.so.
+
+The library is C++/CUDA (kernels for sm_103a, the C ABI of include/ckm.h, and
+the C++ strategy layer that mirrors the reference's AbstractKmeans /
+strategies / factories).  This module only loads it with ctypes and adds thin
+helpers that pass torch device tensors (plumbing for tests and bench.py).
+There is no CPU fallback: every helper raises when the library is missing or
+a call fails.
+
+The directory name has a hyphen, so import it with
+``importlib.import_module("cl-kmeans_gb300")``.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libckm.so")
+BENCH_BIN = os.path.join(_HERE, "bin", "ckm_bench")
+
+MODE_DEFER = 0
+MODE_FINALIZE = 1
+MODE_ACCUMULATE = 2
+
+STATUS = {
+    0: "CKM_OK", -1: "CKM_ERR_INVALID_ARGUMENT", -2: "CKM_ERR_UNSUPPORTED", -3: "CKM_ERR_SCRATCH_TOO_SMALL",
+    -4: "CKM_ERR_CUDA", -5: "CKM_ERR_ALLOC", -6: "CKM_ERR_IO", -7: "CKM_ERR_TIMEOUT",
+    -8: "CKM_ERR_UNKNOWN_STRATEGY", -9: "CKM_ERR_CANCELLED", -10: "CKM_ERR_BUDGET",
+}
+
+# Every symbol include/ckm.h declares (checked by the tests).
+EXPORTS = [
+    "ckm_status_string", "ckm_last_error", "ckm_version", "ckm_device_count", "ckm_launch_count",
+    "ckm_scratch_bytes", "ckm_scratch_init",
+    "ckm_fused_f32", "ckm_fused_f64", "ckm_labeling_f32", "ckm_labeling_f64",
+    "ckm_mass_update_u32", "ckm_mass_update_u64", "ckm_centroid_update_f32", "ckm_centroid_update_f64",
+    "ckm_matrix_divide_row_f32", "ckm_matrix_divide_row_f64", "ckm_matrix_add_f32", "ckm_matrix_add_f64",
+    "ckm_matrix_add_u32", "ckm_matrix_add_u64", "ckm_reduce_vector_parcol_u32",
+    "ckm_finalize_f32", "ckm_finalize_f64", "ckm_generate_mixture_f32",
+    "ckm_kmeans_run_f32", "ckm_kmeans_run_f64",
+]
+
+
+class CkmError(RuntimeError):
+    def __init__(self, status, where, detail=""):
+        self.status = status
+        msg = "%s failed: %s" % (where, STATUS.get(status, status))
+        if detail:
+            msg += " (%s)" % detail
+        super().__init__(msg)
+
+
+class RunConfig(ctypes.Structure):
+    """struct ckm_run_config (include/ckm.h)."""
+    _fields_ = [
+        ("pipeline", ctypes.c_char_p),
+        ("fused_strategy", ctypes.c_char_p),
+        ("labeling_strategy", ctypes.c_char_p),
+        ("mass_update_strategy", ctypes.c_char_p),
+        ("centroid_update_strategy", ctypes.c_char_p),
+        ("device", ctypes.c_int),
+        ("device_budget_bytes", ctypes.c_uint64),
+        ("chunk_bytes", ctypes.c_uint64),
+    ]
+
+
+class RunInfo(ctypes.Structure):
+    """struct ckm_run_info (include/ckm.h)."""
+    _fields_ = [
+        ("total_time_ns", ctypes.c_uint64),
+        ("h2d_bytes", ctypes.c_uint64),
+        ("d2h_bytes", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("iterations", ctypes.c_uint32),
+    ]
+
+
+_lib = None
+
+
+def build(force=False, verbose=False):
+    """Compile libckm.so (and ckm_bench) in-tree for sm_103a."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_ckm_build", os.path.join(_HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force, verbose=verbose)
+
+
+def lib():
+    """The loaded libckm.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libckm.so not built: run __graft_entry__.build() or cl-kmeans_gb300/build.py")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u32, u64, i32, sz = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_size_t
+    sigs = {
+        "ckm_status_string": ([i32], ctypes.c_char_p),
+        "ckm_last_error": ([], ctypes.c_char_p),
+        "ckm_version": ([], i32),
+        "ckm_device_count": ([ctypes.POINTER(ctypes.c_int)], i32),
+        "ckm_launch_count": ([], u64),
+        "ckm_scratch_bytes": ([u32, u32], sz),
+        "ckm_scratch_init": ([vp, sz, vp], i32),
+        "ckm_fused_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
+        "ckm_fused_f64": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
+        "ckm_labeling_f32": ([u32, u64, u32, vp, vp, vp, vp], i32),
+        "ckm_labeling_f64": ([u32, u64, u32, vp, vp, vp, vp], i32),
+        "ckm_mass_update_u32": ([u64, u32, vp, vp, vp], i32),
+        "ckm_mass_update_u64": ([u64, u32, vp, vp, vp], i32),
+        "ckm_centroid_update_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, sz, i32, vp], i32),
+        "ckm_centroid_update_f64": ([u32, u64, u32, vp, vp, vp, vp, vp, sz, i32, vp], i32),
+        "ckm_matrix_divide_row_f32": ([u32, u32, vp, vp, vp], i32),
+        "ckm_matrix_divide_row_f64": ([u32, u32, vp, vp, vp], i32),
+        "ckm_matrix_add_f32": ([u64, vp, vp, vp], i32),
+        "ckm_matrix_add_f64": ([u64, vp, vp, vp], i32),
+        "ckm_matrix_add_u32": ([u64, vp, vp, vp], i32),
+        "ckm_matrix_add_u64": ([u64, vp, vp, vp], i32),
+        "ckm_reduce_vector_parcol_u32": ([u64, u64, vp, vp], i32),
+        "ckm_finalize_f32": ([u32, u32, vp, vp, vp, sz, vp], i32),
+        "ckm_finalize_f64": ([u32, u32, vp, vp, vp, sz, vp], i32),
+        "ckm_generate_mixture_f32": ([u32, u64, u32, u64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, u64, vp, u64, vp], i32),
+        "ckm_kmeans_run_f32": ([ctypes.POINTER(RunConfig), u32, u32, u64, u32, vp, vp, vp, vp,
+                                ctypes.POINTER(RunInfo)], i32),
+        "ckm_kmeans_run_f64": ([ctypes.POINTER(RunConfig), u32, u32, u64, u32, vp, vp, vp, vp,
+                                ctypes.POINTER(RunInfo)], i32),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return _lib
+
+
+def check(status, where):
+    if status != 0:
+        detail = lib().ckm_last_error()
+        raise CkmError(status, where, detail.decode() if detail else "")
+    return status
+
+
+# ----------------------------------------------------------------------------
+# torch plumbing (device memory and streams only)
+# ----------------------------------------------------------------------------
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def scratch_bytes(d, k):
+    return int(lib().ckm_scratch_bytes(d, k))
+
+
+def new_scratch(d, k, device="cuda"):
+    """Zeroed FP64 merge scratch for (d, k) as a torch uint8 tensor."""
+    import torch
+    t = torch.empty(scratch_bytes(d, k), dtype=torch.uint8, device=device)
+    check(lib().ckm_scratch_init(_p(t), t.numel(), _stream()), "ckm_scratch_init")
+    return t
+
+
+def _is64(t):
+    import torch
+    return t.dtype == torch.float64
+
+
+def fused(points, old_centroids, new_centroids, labels, masses, scratch, n, d, k, mode=MODE_FINALIZE,
+          stream=None):
+    """ckm_fused_{f32,f64}: label + mass + sums (+ divide) in one launch."""
+    fn = lib().ckm_fused_f64 if _is64(points) else lib().ckm_fused_f32
+    check(fn(d, n, k, _p(points), _p(old_centroids), _p(new_centroids), _p(labels), _p(masses), _p(scratch),
+             scratch.numel(), mode, _stream(stream)), "ckm_fused")
+
+
+def labeling(points, centroids, labels, n, d, k, stream=None):
+    fn = lib().ckm_labeling_f64 if _is64(points) else lib().ckm_labeling_f32
+    check(fn(d, n, k, _p(points), _p(centroids), _p(labels), _stream(stream)), "ckm_labeling")
+
+
+def mass_update(labels, masses, n, k, stream=None):
+    import torch
+    fn = lib().ckm_mass_update_u64 if labels.dtype in (torch.int64, torch.uint64) else lib().ckm_mass_update_u32
+    check(fn(n, k, _p(labels), _p(masses), _stream(stream)), "ckm_mass_update")
+
+
+def centroid_update(points, centroids, labels, masses, scratch, n, d, k, mode=MODE_ACCUMULATE, stream=None):
+    fn = lib().ckm_centroid_update_f64 if _is64(points) else lib().ckm_centroid_update_f32
+    check(fn(d, n, k, _p(points), _p(centroids), _p(labels), _p(masses), _p(scratch), scratch.numel(), mode,
+             _stream(stream)), "ckm_centroid_update")
+
+
+def finalize(centroids, masses, scratch, d, k, stream=None):
+    fn = lib().ckm_finalize_f64 if _is64(centroids) else lib().ckm_finalize_f32
+    check(fn(d, k, _p(centroids), _p(masses), _p(scratch), scratch.numel(), _stream(stream)), "ckm_finalize")
+
+
+def divide_row(matrix, masses, d, k, stream=None):
+    fn = lib().ckm_matrix_divide_row_f64 if _is64(matrix) else lib().ckm_matrix_divide_row_f32
+    check(fn(d, k, _p(matrix), _p(masses), _stream(stream)), "ckm_matrix_divide_row")
+
+
+def reduce_vector_parcol(data, num_cols, num_rows, stream=None):
+    check(lib().ckm_reduce_vector_parcol_u32(num_cols, num_rows, _p(data), _stream(stream)),
+          "ckm_reduce_vector_parcol_u32")
+
+
+def generate_mixture(points, n, d, blobs, seed, center=(-10.0, 10.0), sigma=(1.0, 1.0), first_point=0,
+                     stride=None, stream=None):
+    """Fills a column-major float32 device tensor with the seeded mixture."""
+    check(lib().ckm_generate_mixture_f32(d, n, blobs, seed, center[0], center[1], sigma[0], sigma[1], first_point,
+                                         _p(points), n if stride is None else stride, _stream(stream)),
+          "ckm_generate_mixture_f32")
+
+
+def launch_count():
+    return int(lib().ckm_launch_count())
+
+
+def kmeans_run(points, d, k, iterations, centroids, pipeline="single_stage", fused_strategy="feature_sum",
+               labeling_strategy="unroll_vector", mass_update_strategy="part_local",
+               centroid_update_strategy="feature_sum", device=0, device_budget_bytes=0, chunk_bytes=0,
+               masses=None, labels=None):
+    """AbstractKmeans::operator() over HOST numpy arrays (column-major flat
+    points and centroids).  Returns (centroids, masses, labels, RunInfo)."""
+    import numpy as np
+    f64 = points.dtype == np.float64
+    P = np.ascontiguousarray(points, np.float64 if f64 else np.float32)
+    n = P.size // d
+    C = np.array(centroids, np.float64 if f64 else np.float32, copy=True)
+    it = np.uint64 if f64 else np.uint32
+    M = np.zeros(k, it) if masses is None else masses
+    Lb = np.zeros(n, it) if labels is None else labels
+    cfg = RunConfig(pipeline.encode(), fused_strategy.encode(), labeling_strategy.encode(),
+                    mass_update_strategy.encode(), centroid_update_strategy.encode(), device,
+                    device_budget_bytes, chunk_bytes)
+    info = RunInfo()
+    fn = lib().ckm_kmeans_run_f64 if f64 else lib().ckm_kmeans_run_f32
+    check(fn(ctypes.byref(cfg), iterations, d, n, k, P.ctypes.data, C.ctypes.data, M.ctypes.data,
+             Lb.ctypes.data, ctypes.byref(info)), "ckm_kmeans_run")
+    return C, M, Lb, info

@@ -1,0 +1,118 @@
+// Device-side helpers shared by the kernels: packed FP32x2 arithmetic,
+// warp reductions and the FP64 scratch finalisation every fused / centroid
+// update launch ends with.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "ckm_internal.h"
+
+namespace ckm {
+
+// --- packed FP32x2 (sm_100 family): two IEEE round-to-nearest operations per
+// instruction.  Each lane of the pair rounds exactly like the scalar op, so
+// the distance keeps the reference's fma(t, t, acc) bit pattern.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rr;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rr, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rr;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rr, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rc, rr;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rr, ra, rb, rc;\n\t"
+        "mov.b64 {%0, %1}, rr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+
+__device__ __forceinline__ float warp_sum_f32(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_f64(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Type maximum used as the argmin's starting value (the reference's
+// CL_POINT_MAX / std::numeric_limits<PointT>::max()).
+template <typename T> struct TypeMax;
+template <> struct TypeMax<float> { static __device__ __forceinline__ float v() { return FLT_MAX; } };
+template <> struct TypeMax<double> { static __device__ __forceinline__ double v() { return DBL_MAX; } };
+
+// Takes a ticket after this CTA merged its partials; returns true in the one
+// CTA that arrives last (all other CTAs' FP64 atomics are then visible).
+__device__ __forceinline__ bool last_cta_ticket(unsigned int* counter) {
+    __shared__ unsigned int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(counter, 1u);
+        s_last = (t == gridDim.x - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    bool last = s_last != 0;
+    if (last) __threadfence();
+    return last;
+}
+
+// Turns the FP64 scratch into the call's outputs and re-zeroes it.
+//   FINALIZE:   C = sums / masses (0/0 -> NaN), masses = counts
+//   ACCUMULATE: C += sums, masses += counts      (reference functor contract)
+// Run by every thread of one CTA.
+template <typename T, typename M>
+__device__ void finalize_block(uint32_t d, uint32_t k, T* C, M* masses, ScratchView sv, int mode) {
+    const uint64_t kd = (uint64_t)k * d;
+    for (uint64_t e = threadIdx.x; e < kd; e += blockDim.x) {
+        const uint32_t c = (uint32_t)(e % k);
+        const double s = __ldcg(&sv.sums[e]);
+        if (mode == CKM_MODE_FINALIZE) {
+            const double m = (double)__ldcg(&sv.masses[c]);
+            C[e] = (T)(s / m);
+        } else {
+            C[e] = C[e] + (T)s;
+        }
+        sv.sums[e] = 0.0;
+    }
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
+        const unsigned long long m = __ldcg(&sv.masses[c]);
+        if (masses != nullptr) {  // the centroid-update pass leaves masses alone
+            if (mode == CKM_MODE_FINALIZE) masses[c] = (M)m;
+            else masses[c] = masses[c] + (M)m;
+        }
+        sv.masses[c] = 0ull;
+    }
+    if (threadIdx.x == 0) sv.ctrl[0] = 0u;
+}
+
+}  // namespace ckm

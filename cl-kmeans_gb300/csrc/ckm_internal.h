@@ -1,0 +1,100 @@
+// Internal declarations shared by the CUDA translation units and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/ckm.h"
+
+namespace ckm {
+
+// Last-error message of the calling host thread.
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t err, const char* where);
+
+// Scratch layout (all offsets 256-byte aligned):
+//   sums     double[k * d]   column-major like the centroids (f * k + c)
+//   masses   uint64[k]
+//   control  uint32[64]      [0] CTA arrival ticket, [1] error flag
+struct ScratchLayout {
+    size_t sums_off, mass_off, ctrl_off, total;
+};
+ScratchLayout scratch_layout(uint32_t d, uint32_t k);
+
+struct ScratchView {
+    double* sums;
+    unsigned long long* masses;
+    unsigned int* ctrl;
+};
+inline ScratchView scratch_view(void* base, const ScratchLayout& L) {
+    char* b = static_cast<char*>(base);
+    return ScratchView{reinterpret_cast<double*>(b + L.sums_off),
+                       reinterpret_cast<unsigned long long*>(b + L.mass_off),
+                       reinterpret_cast<unsigned int*>(b + L.ctrl_off)};
+}
+
+// Counts kernel launches made by this library (for the run info and bench).
+void count_launch(uint64_t n = 1);
+uint64_t launch_count();
+
+// Device properties cached per device.
+struct DeviceInfo {
+    int sm_count;
+    size_t smem_optin;
+    int cc_major, cc_minor;
+};
+const DeviceInfo& device_info();
+
+// Work of one fused / labeling / centroid-update launch (f32).
+struct FusedF32 {
+    const float* points;
+    const float* centroids;       // old centroids (column-major)
+    uint32_t* labels;             // written by fused / labeling; read by centroid update
+    float* new_centroids;         // FINALIZE: means, ACCUMULATE: += sums
+    uint32_t* masses;             // FINALIZE: counts, ACCUMULATE: += counts
+    ScratchView scratch;
+    uint64_t n;
+    uint32_t d, k;
+    int mode;
+};
+
+struct FusedF64 {
+    const double* points;
+    const double* centroids;
+    uint64_t* labels;
+    double* new_centroids;
+    uint64_t* masses;
+    ScratchView scratch;
+    uint64_t n;
+    uint32_t d, k;
+    int mode;
+};
+
+enum class Pass { Fused, LabelOnly, SumsOnly };
+
+// Launchers (return CKM_OK or an error status; never throw).
+int launch_fused_f32(const FusedF32& a, Pass pass, cudaStream_t s);
+int launch_generic_f32(const FusedF32& a, Pass pass, cudaStream_t s);
+int launch_generic_f64(const FusedF64& a, Pass pass, cudaStream_t s);
+bool lowd_supported(uint32_t d, uint32_t k);
+
+int launch_finalize_f32(uint32_t d, uint32_t k, float* c, uint32_t* m, ScratchView sv, int mode,
+                        cudaStream_t s);
+int launch_finalize_f64(uint32_t d, uint32_t k, double* c, uint64_t* m, ScratchView sv, int mode,
+                        cudaStream_t s);
+int launch_mass_u32(uint64_t n, uint32_t k, const uint32_t* labels, uint32_t* masses, cudaStream_t s);
+int launch_mass_u64(uint64_t n, uint32_t k, const uint64_t* labels, uint64_t* masses, cudaStream_t s);
+int launch_divide_f32(uint32_t d, uint32_t k, float* m, const uint32_t* masses, cudaStream_t s);
+int launch_divide_f64(uint32_t d, uint32_t k, double* m, const uint64_t* masses, cudaStream_t s);
+template <typename T>
+int launch_add(uint64_t count, T* a, const T* b, cudaStream_t s);
+int launch_reduce_parcol_u32(uint64_t cols, uint64_t rows, uint32_t* data, cudaStream_t s);
+int launch_generate_f32(uint32_t d, uint64_t n, uint32_t blobs, uint64_t seed, float clo, float chi,
+                        float slo, float shi, uint64_t first, float* out, uint64_t stride,
+                        cudaStream_t s);
+
+}  // namespace ckm

@@ -1,0 +1,226 @@
+/*
+ * ckm.h -- C ABI of the GB300 Lloyd k-means library (libckm.so).
+ *
+ * Drop-in boundary for the reference's Lloyd iteration path.  The reference
+ * binds its kernels through C++ std::function factories over Boost.Compute
+ * buffers; each entry point below replaces one of those functors (the
+ * replaced interface is cited at each declaration).  Everything is plain
+ * pointers, sizes and a CUDA stream; nothing allocates on the hot calls.
+ *
+ * Layouts follow the reference (lloyd_fused_feature_sum.cl:77-79, 200, 230):
+ *   points     column-major  P[f * num_points + p]      (PointT)
+ *   centroids  column-major  C[f * num_clusters + c]    (PointT)
+ *   labels     LabelT[num_points]
+ *   masses     MassT[num_clusters]
+ * Type pairs: float/uint32/uint32 (_f32) and double/uint64/uint64 (_f64),
+ * the two instantiations bench.cpp:469-503 dispatches.
+ *
+ * Semantics kept from the reference:
+ *   - distance = fma(x_f - c_f, x_f - c_f, acc) over f = 0..d-1 from 0,
+ *     argmin with strict '<' from cluster 0 with min = type max and label 0:
+ *     the lowest index wins a tie and a NaN distance never wins
+ *     (kmeans_naive.cpp:48-63, lloyd_fused_feature_sum.cl:209-239);
+ *   - an empty cluster divides 0 by 0 and gets NaN centroids
+ *     (kmeans_naive.cpp:96-100, matrix_binary_op.cl:98-114);
+ *   - functor-level calls ACCUMULATE into new_centroids / masses, the caller
+ *     zero-fills (kmeans_single_stage.hpp:97-112, fused_feature_sum.hpp:403-439).
+ *
+ * Every function returns a status: CKM_OK (0) or a negative ckm_status.  No
+ * exception crosses this boundary; ckm_last_error() has the message.
+ */
+#ifndef CKM_H
+#define CKM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ABI-identical to cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st *ckm_stream_t;
+
+typedef enum ckm_status {
+    CKM_OK = 0,
+    CKM_ERR_INVALID_ARGUMENT = -1,  /* the reference's size asserts, fused_feature_sum.hpp:210-220 */
+    CKM_ERR_UNSUPPORTED = -2,
+    CKM_ERR_SCRATCH_TOO_SMALL = -3,
+    CKM_ERR_CUDA = -4,
+    CKM_ERR_ALLOC = -5,
+    CKM_ERR_IO = -6,
+    CKM_ERR_TIMEOUT = -7,           /* a bounded device wait ran out */
+    CKM_ERR_UNKNOWN_STRATEGY = -8,  /* the factories' std::invalid_argument(strategy) */
+    CKM_ERR_CANCELLED = -9,
+    CKM_ERR_BUDGET = -10            /* device-memory budget would be exceeded */
+} ckm_status;
+
+/* Fused-call modes.  CKM_MODE_ACCUMULATE is the reference FusedFunction
+ * contract (+= into new_centroids sums and masses).  CKM_MODE_FINALIZE runs a
+ * whole Lloyd iteration in one launch: new_centroids = means, masses = counts
+ * (what fill -> fused -> reduce -> add -> matrix_divide.row computes,
+ * kmeans_single_stage.hpp:97-144).  CKM_MODE_DEFER only accumulates into the
+ * FP64 scratch; ckm_finalize_* turns it into centroids later (chunked runs). */
+enum {
+    CKM_MODE_DEFER = 0,
+    CKM_MODE_FINALIZE = 1,
+    CKM_MODE_ACCUMULATE = 2
+};
+
+const char *ckm_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *ckm_last_error(void);
+/* Library ABI version (major * 10000 + minor * 100 + patch). */
+int ckm_version(void);
+/* Number of CUDA devices the library sees (CKM_ERR_CUDA when none). */
+int ckm_device_count(int *count);
+/* Kernels this library has launched in this process (all threads). */
+uint64_t ckm_launch_count(void);
+
+/* ---------------------------------------------------------------------- */
+/* Scratch.  The fused, centroid-update and finalize calls merge per-CTA   */
+/* partial sums in FP64 into caller-owned scratch (this replaces the        */
+/* reference's global partial buffers + ReduceVectorParcol,                */
+/* fused_feature_sum.hpp:224-307, 391-425).  Size it with                   */
+/* ckm_scratch_bytes, zero it once with ckm_scratch_init; every call that   */
+/* finalizes or accumulates leaves it zeroed again.  Calls that share one   */
+/* scratch must be stream-ordered.                                          */
+/* ---------------------------------------------------------------------- */
+size_t ckm_scratch_bytes(uint32_t num_features, uint32_t num_clusters);
+int ckm_scratch_init(void *scratch, size_t scratch_bytes, ckm_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Fused single pass: label + mass + feature sums (+ merge, + divide).      */
+/* Replaces FusedFactory::FusedFunction (fused_factory.hpp:34-53), i.e.     */
+/* FusedFeatureSum::operator() (cl_kernels/fused_feature_sum.hpp:191-444)   */
+/* and FusedClusterMerge::operator() (cl_kernels/fused_cluster_merge.hpp:   */
+/* 193-414).                                                                */
+/* ---------------------------------------------------------------------- */
+int ckm_fused_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                  const float *points, const float *old_centroids, float *new_centroids,
+                  uint32_t *labels, uint32_t *masses, void *scratch, size_t scratch_bytes,
+                  int mode, ckm_stream_t stream);
+int ckm_fused_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                  const double *points, const double *old_centroids, double *new_centroids,
+                  uint64_t *labels, uint64_t *masses, void *scratch, size_t scratch_bytes,
+                  int mode, ckm_stream_t stream);
+
+/* Labels only.  Replaces LabelingFactory::LabelingFunction
+ * (labeling_factory.hpp:33-48) = LabelingUnrollVector::operator()
+ * (cl_kernels/labeling_unroll_vector.hpp:168-272). */
+int ckm_labeling_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                     const float *points, const float *centroids, uint32_t *labels,
+                     ckm_stream_t stream);
+int ckm_labeling_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                     const double *points, const double *centroids, uint64_t *labels,
+                     ckm_stream_t stream);
+
+/* Label histogram, += into masses.  Replaces
+ * MassUpdateFactory::MassUpdateFunction (mass_update_factory.hpp:36-48) for
+ * all four strategies (cl_kernels/mass_update_{global_atomic,part_global,
+ * part_local,part_private}.hpp).  Exact integer counts. */
+int ckm_mass_update_u32(uint64_t num_points, uint32_t num_clusters, const uint32_t *labels,
+                        uint32_t *masses, ckm_stream_t stream);
+int ckm_mass_update_u64(uint64_t num_points, uint32_t num_clusters, const uint64_t *labels,
+                        uint64_t *masses, ckm_stream_t stream);
+
+/* Per-label feature sums, += into centroids (the caller zero-fills and then
+ * divides).  Replaces CentroidUpdateFactory::CentroidUpdateFunction
+ * (centroid_update_factory.hpp:37-54) for feature_sum, feature_sum_pardim
+ * and cluster_merge (cl_kernels/centroid_update_*.hpp).  `masses` is the
+ * reference argument and is not modified.  mode CKM_MODE_DEFER keeps the
+ * sums in scratch (for chunked runs), CKM_MODE_ACCUMULATE adds them into
+ * centroids (reference contract). */
+int ckm_centroid_update_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                            const float *points, float *centroids, const uint32_t *labels,
+                            const uint32_t *masses, void *scratch, size_t scratch_bytes,
+                            int mode, ckm_stream_t stream);
+int ckm_centroid_update_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                            const double *points, double *centroids, const uint64_t *labels,
+                            const uint64_t *masses, void *scratch, size_t scratch_bytes,
+                            int mode, ckm_stream_t stream);
+
+/* M[f*k + c] = M[f*k + c] / (PointT) masses[c].  Replaces
+ * MatrixBinaryOp<PointT,MassT>::row with Divide
+ * (cl_kernels/matrix_binary_op.hpp:86-127; matrix_binary_op.cl:98-114). */
+int ckm_matrix_divide_row_f32(uint32_t num_features, uint32_t num_clusters, float *matrix,
+                              const uint32_t *masses, ckm_stream_t stream);
+int ckm_matrix_divide_row_f64(uint32_t num_features, uint32_t num_clusters, double *matrix,
+                              const uint64_t *masses, ckm_stream_t stream);
+
+/* A[i] += B[i].  Replaces MatrixBinaryOp::matrix with Add
+ * (cl_kernels/matrix_binary_op.hpp:149-188; matrix_binary_op.cl:126-140). */
+int ckm_matrix_add_f32(uint64_t count, float *a, const float *b, ckm_stream_t stream);
+int ckm_matrix_add_f64(uint64_t count, double *a, const double *b, ckm_stream_t stream);
+int ckm_matrix_add_u32(uint64_t count, uint32_t *a, const uint32_t *b, ckm_stream_t stream);
+int ckm_matrix_add_u64(uint64_t count, uint64_t *a, const uint64_t *b, ckm_stream_t stream);
+
+/* Column sums of `num_cols` vectors of `num_rows` uint32 (column-major),
+ * wrapping mod 2^32, into the first num_rows entries of `data`.  Replaces
+ * ReduceVectorParcol (cl_kernels/reduce_vector_parcol.hpp:64-155), which the
+ * reference's test/reduce_vector.cpp pins. */
+int ckm_reduce_vector_parcol_u32(uint64_t num_cols, uint64_t num_rows, uint32_t *data,
+                                 ckm_stream_t stream);
+
+/* Turns the FP64 sums of CKM_MODE_DEFER calls into centroids and masses
+ * (centroids = sums / masses; 0/0 -> NaN) and re-zeroes the scratch.  The
+ * matrix_divide.row step of the buffered strategies
+ * (kmeans_single_stage_buffered.hpp:230-244). */
+int ckm_finalize_f32(uint32_t num_features, uint32_t num_clusters, float *new_centroids,
+                     uint32_t *masses, void *scratch, size_t scratch_bytes, ckm_stream_t stream);
+int ckm_finalize_f64(uint32_t num_features, uint32_t num_clusters, double *new_centroids,
+                     uint64_t *masses, void *scratch, size_t scratch_bytes, ckm_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Seeded synthetic Gaussian mixture (counter-based Philox4x32-10), column- */
+/* major, generated on the device.  Stands in for the reference's           */
+/* cluster_generator.cpp:157-196 file writer.  Blob centres are uniform in  */
+/* [center_lo, center_hi]^d, blob sigmas uniform in [sigma_lo, sigma_hi],   */
+/* components equally likely; point p depends only on (seed, p).            */
+/* ---------------------------------------------------------------------- */
+int ckm_generate_mixture_f32(uint32_t num_features, uint64_t num_points, uint32_t num_blobs,
+                             uint64_t seed, float center_lo, float center_hi, float sigma_lo,
+                             float sigma_hi, uint64_t first_point, float *points,
+                             uint64_t points_stride, ckm_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Host-level run: AbstractKmeans<PointT,LabelT,MassT>::operator()          */
+/* (abstract_kmeans.hpp:106-130) through a C ABI, with HOST buffers.  The   */
+/* pipeline and per-stage strategies take the reference's .conf names.      */
+/* ---------------------------------------------------------------------- */
+typedef struct ckm_run_config {
+    const char *pipeline;                  /* single_stage | single_stage_buffered |
+                                              three_stage | three_stage_buffered */
+    const char *fused_strategy;            /* feature_sum | cluster_merge */
+    const char *labeling_strategy;         /* unroll_vector */
+    const char *mass_update_strategy;      /* global_atomic | part_global | part_local | part_private */
+    const char *centroid_update_strategy;  /* feature_sum | feature_sum_pardim | cluster_merge */
+    int device;                            /* CUDA device ordinal */
+    uint64_t device_budget_bytes;          /* buffered pipelines: device-memory cap (0 = auto) */
+    uint64_t chunk_bytes;                  /* buffered pipelines: points bytes per chunk (0 = auto) */
+} ckm_run_config;
+
+typedef struct ckm_run_info {
+    uint64_t total_time_ns;      /* the reference's TotalTime window (iteration loop) */
+    uint64_t h2d_bytes;          /* host -> device bytes moved by the call */
+    uint64_t d2h_bytes;          /* device -> host bytes moved by the call */
+    uint64_t kernel_launches;    /* kernels this library launched */
+    uint32_t iterations;         /* iterations run */
+} ckm_run_info;
+
+/* centroids: in = initial, out = final (k = num_clusters).  masses, labels:
+ * out.  info may be NULL. */
+int ckm_kmeans_run_f32(const ckm_run_config *config, uint32_t max_iterations,
+                       uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                       const float *host_points, float *host_centroids, uint32_t *host_masses,
+                       uint32_t *host_labels, ckm_run_info *info);
+int ckm_kmeans_run_f64(const ckm_run_config *config, uint32_t max_iterations,
+                       uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                       const double *host_points, double *host_centroids, uint64_t *host_masses,
+                       uint64_t *host_labels, ckm_run_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CKM_H */

@@ -1,0 +1,166 @@
+"""Three-stage functors and the host-level pipelines (ckm_kmeans_run_*),
+each against the oracle.
+
+The three-stage functors follow the reference contracts: labeling writes
+labels (labeling_factory.hpp:33-48); mass update adds counts into masses
+(mass_update_factory.hpp:36-48); centroid update adds per-label sums into the
+zero-filled centroids (centroid_update_factory.hpp:37-54); divide is
+MatrixBinaryOp::row (matrix_binary_op.cl:98-114).  The pipelines are
+AbstractKmeans::operator() for the four `kmeans.pipeline` names
+(bench.cpp:319-404) with host arrays.
+"""
+import numpy as np
+import pytest
+
+from conftest import blobs
+from test_fused_gpu import check_centroids, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,d,k", [(40000, 4, 16), (9999, 3, 5), (5000, 24, 30), (20000, 2, 300)])
+def test_three_stage_functors(ckm, oracle, cuda, n, d, k):
+    import torch
+    P = blobs(n, d, k, seed=n + d)
+    C = oracle.first_x_f32(P, n, d, k)
+    dP, dC = to_dev(P, cuda), to_dev(C, cuda)
+    dL = torch.zeros(n, dtype=torch.int32, device=cuda)
+    ckm.labeling(dP, dC, dL, n, d, k)
+    torch.cuda.synchronize()
+    ref = oracle.label_f32(P, n, d, k, C)
+    assert np.array_equal(dL.cpu().numpy().view(np.uint32), ref)
+
+    dM = torch.full((k,), 5, dtype=torch.int32, device=cuda)
+    ckm.mass_update(dL, dM, n, k)
+    torch.cuda.synchronize()
+    assert np.array_equal(dM.cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k) + 5)
+
+    dS = torch.zeros(k * d, dtype=torch.float32, device=cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    ckm.centroid_update(dP, dS, dL, dM, S, n, d, k, ckm.MODE_ACCUMULATE)
+    torch.cuda.synchronize()
+    sums, masses = oracle.sums_f64(P, n, d, k, ref)
+    assert np.allclose(dS.cpu().numpy(), sums, rtol=2e-6, atol=2e-6 * np.abs(P).max() * 10)
+
+    dM2 = torch.from_numpy(masses.astype(np.uint32).view(np.int32)).to(cuda)
+    ckm.divide_row(dS, dM2, d, k)
+    torch.cuda.synchronize()
+    check_centroids(oracle, P, n, d, k, ref, dS.cpu().numpy())
+
+
+def test_mass_update_exact_uniform_labels(ckm, cuda):
+    """The reference's histogram test (test/histogram.cpp:31-39, 211-226):
+    exact counts of 1 Mi uniform labels for 2..16 bins."""
+    import torch
+    rng = np.random.default_rng(3)
+    n = 1 << 20
+    for k in (2, 4, 8, 16):
+        labels = rng.integers(0, k, size=n).astype(np.uint32)
+        dL = to_dev(labels.view(np.int32), cuda)
+        dM = torch.zeros(k, dtype=torch.int32, device=cuda)
+        ckm.mass_update(dL, dM, n, k)
+        torch.cuda.synchronize()
+        assert np.array_equal(dM.cpu().numpy().view(np.uint32), np.bincount(labels, minlength=k))
+
+
+@pytest.mark.parametrize("rows,cols,kind", [(4, 256, "ascending"), (4, 256, "large"), (4, 256, "random"),
+                                            (4, 65536, "random"), (2048, 65536, "random"),
+                                            (256, 46080, "random"), (4, 57344, "random")])
+def test_reduce_vector_parcol_exact(ckm, cuda, rows, cols, kind):
+    """The reference's ReduceVectorParcol shapes (test/reduce_vector.cpp:74-221),
+    uint32 column sums wrapping mod 2^32."""
+    import torch
+    rng = np.random.default_rng(rows * cols)
+    if kind == "ascending":
+        data = np.arange(rows * cols, dtype=np.uint32)
+    elif kind == "large":
+        data = np.full(rows * cols, 1 << 31, dtype=np.uint32)
+    else:
+        data = rng.integers(0, 1 << 32, size=rows * cols, dtype=np.uint64).astype(np.uint32)
+    want = data.reshape(cols, rows).astype(np.uint64).sum(axis=0) % (1 << 32)
+    dD = to_dev(data.view(np.int32), cuda)
+    ckm.reduce_vector_parcol(dD, cols, rows)
+    torch.cuda.synchronize()
+    assert np.array_equal(dD[:rows].cpu().numpy().view(np.uint32), want.astype(np.uint32))
+
+
+def _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L):
+    """End-to-end against the oracle's FP32 KmeansNaive restatement: labels
+    equal except where the FP64 top-two gap under the oracle's last input
+    centroids is tiny (a near tie whose side depends on ulp-level centroid
+    differences); masses equal the counts of our labels; centroids are the
+    FP64 means of our labels."""
+    Cr, Mr, Lr = oracle.lloyd_f32(P, n, d, k, iters, C0)
+    mism = np.nonzero(L != Lr)[0]
+    if mism.size:
+        Cprev, _, _ = oracle.lloyd_f32(P, n, d, k, iters - 1, C0)
+        _, gap, best = oracle.label_gap_f64(P, n, d, k, Cprev)
+        rel = gap[mism] / np.maximum(best[mism], 1e-30)
+        assert mism.size <= max(3, n // 10000), "too many label mismatches: %d" % mism.size
+        assert np.all(rel < 1e-3), "mismatch with a large FP64 gap"
+    assert np.array_equal(M, oracle.mass_u32(L, k))
+    check_centroids(oracle, P, n, d, k, L, C)
+
+
+@pytest.mark.parametrize("pipeline", ["single_stage", "three_stage", "single_stage_buffered",
+                                      "three_stage_buffered"])
+def test_pipelines_end_to_end(ckm, oracle, cuda, pipeline):
+    n, d, k, iters = 100003, 4, 10, 12
+    P = blobs(n, d, k, seed=99)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    extra = {}
+    if pipeline.endswith("buffered"):
+        # force streaming: 5 chunks of 24k points; the budget holds the 3
+        # streaming slots plus 2 resident chunks (+ the fixed 1 MiB reserve)
+        extra = dict(chunk_bytes=24000 * d * 4, device_budget_bytes=(24000 * (d + 1) * 4) * 5 + (1 << 20) + 65536)
+    C, M, L, info = ckm.kmeans_run(P, d, k, iters, C0, pipeline=pipeline, **extra)
+    assert info.iterations == iters and info.kernel_launches > 0
+    _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L)
+
+
+def test_pipeline_double_types(ckm, oracle, cuda):
+    n, d, k, iters = 20000, 3, 6, 5
+    P = blobs(n, d, k, seed=98).astype(np.float64)
+    C0 = oracle.first_x_f32(P.astype(np.float32), n, d, k).astype(np.float64)
+    for pipeline in ("single_stage", "three_stage", "single_stage_buffered", "three_stage_buffered"):
+        C, M, L, _ = ckm.kmeans_run(P, d, k, iters, C0, pipeline=pipeline,
+                                    chunk_bytes=(6000 * d * 8 if "buffered" in pipeline else 0))
+        Cr, Mr, Lr = oracle.lloyd_f64(P, n, d, k, iters, C0)
+        assert np.array_equal(L, Lr), pipeline
+        assert np.array_equal(M, Mr), pipeline
+        assert np.allclose(C, Cr, rtol=1e-12, atol=1e-12), pipeline
+
+
+def test_unknown_strategy_is_rejected(ckm, cuda):
+    P = blobs(1000, 2, 3, seed=1)
+    C0 = P.reshape(2, 1000)[:, :3].copy().reshape(-1)
+    with pytest.raises(ckm.CkmError) as e:
+        ckm.kmeans_run(P, 2, 3, 1, C0, pipeline="single_stage", fused_strategy="no_such_strategy")
+    assert e.value.status == -8
+    with pytest.raises(ckm.CkmError) as e:
+        ckm.kmeans_run(P, 2, 3, 1, C0, pipeline="three_stage", mass_update_strategy="bogus")
+    assert e.value.status == -8
+    with pytest.raises(ckm.CkmError) as e:
+        ckm.kmeans_run(P, 2, 3, 1, C0, pipeline="warp_drive")
+    assert e.value.status == -8
+
+
+def test_generator_is_deterministic_and_chunkable(ckm, cuda):
+    import torch
+    n, d = 100000, 5
+    a = torch.empty(n * d, dtype=torch.float32, device=cuda)
+    b = torch.empty(n * d, dtype=torch.float32, device=cuda)
+    ckm.generate_mixture(a, n, d, 16, seed=42, sigma=(0.5, 2.0))
+    ckm.generate_mixture(b, n, d, 16, seed=42, sigma=(0.5, 2.0))
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    # the second half generated on its own (first_point offset, row stride n)
+    c = torch.zeros(n * d, dtype=torch.float32, device=cuda)
+    half = n // 2
+    ckm.generate_mixture(c[half:], n - half, d, 16, seed=42, sigma=(0.5, 2.0), first_point=half, stride=n)
+    torch.cuda.synchronize()
+    A = a.view(d, n)[:, half:]
+    C = c.view(d, n)[:, half:]
+    assert torch.equal(A, C)
+    x = a.cpu().numpy()
+    assert np.isfinite(x).all() and np.abs(x).max() < 40.0
