@@ -39,6 +39,8 @@ WORKLOADS = {
     # name: (n, d, k, blobs, sigma_lo, sigma_hi, iterations of the configured run)
     "lloyd_n2^28_d4_k16": (1 << 28, 4, 16, 16, 0.5, 2.0, 50),
     "lloyd_n2^20_d4_k10": (1 << 20, 4, 10, 10, 1.0, 1.0, 30),
+    # profiling-size case of the default workload: 160 MB of inputs (> L2)
+    "lloyd_n2^25_d4_k16": (1 << 25, 4, 16, 16, 0.5, 2.0, 50),
 }
 DEFAULT_WORKLOAD = "lloyd_n2^28_d4_k16"
 SEED = 42
@@ -287,7 +289,7 @@ def main():
 
     # --- e2e through the C ABI with pinned host buffers --------------------
     e2e = None
-    if True:
+    if args.e2e_steps > 0:
         hostP = torch.empty(n * d, dtype=torch.float32, pin_memory=True)
         hostP.copy_(P)
         hp = hostP.numpy()

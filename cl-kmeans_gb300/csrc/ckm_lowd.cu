@@ -282,11 +282,17 @@ int launch_lowd_t(const FusedF32& a, cudaStream_t s) {
         std::lock_guard<std::mutex> g(C.mu);
         const void* key = reinterpret_cast<const void*>(kern);
         auto it = C.attr_set.find(key);
-        if (it == C.attr_set.end() || (size_t)it->second < smem) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)di.smem_optin);
+        if (it == C.attr_set.end()) {
+            // the dynamic limit is the opt-in maximum minus the static shared memory
+            cudaFuncAttributes fa;
+            cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(lowd)");
+            const int dyn_max = (int)(di.smem_optin - fa.sharedSizeBytes);
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_max);
             if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(lowd)");
-            C.attr_set[key] = (int)di.smem_optin;
+            it = C.attr_set.emplace(key, dyn_max).first;
         }
+        if ((size_t)it->second < smem) return fail(CKM_ERR_UNSUPPORTED, "lowd: shared-memory table too large");
         const uint64_t okey = (reinterpret_cast<uint64_t>(key) << 20) ^ (uint64_t)smem;
         auto oi = C.occ.find(okey);
         if (oi == C.occ.end()) {
