@@ -21,6 +21,7 @@
 #include "ckm_device.cuh"
 #include "ckm_internal.h"
 
+#include <cstdlib>
 #include <mutex>
 #include <unordered_map>
 
@@ -32,6 +33,10 @@ constexpr int BLK = 256;
 template <int D> struct LowdCfg {
     static constexpr int PPT = D <= 4 ? 8 : (D <= 8 ? 4 : 2);  // points per thread per tile
     static constexpr int VW = PPT < 4 ? PPT : 4;                 // floats per vector load
+};
+
+template <int D> struct AccVec {
+    static constexpr int VG = (D % 4 == 0) ? 4 : ((D % 2 == 0) ? 2 : 1);  // floats per table vector
 };
 
 template <int D, int PPT>
@@ -87,7 +92,7 @@ __device__ __forceinline__ void load_tile(Tile<D, PPT>& T, const FusedF32& a, ui
     }
 }
 
-template <int D, int PPT, int ACC, Pass PASS>
+template <int D, int PPT, int ACC, Pass PASS, int NT>
 __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a, uint64_t p0, bool vec,
                                              const float2* __restrict__ s_c, float* __restrict__ s_acc) {
     constexpr int VW = LowdCfg<D>::VW;
@@ -147,16 +152,53 @@ __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a,
     }
 
     if constexpr (PASS != Pass::LabelOnly) {
-        if constexpr (ACC == 0) {
+        if constexpr (ACC == 3) {
+            // private rows of VG-wide vectors: one vector load, packed adds and
+            // one vector store per VG features, masses in their own column
+            constexpr int VG = AccVec<D>::VG;
+            constexpr int G = D / VG;
+            float* srow0 = s_acc + (size_t)threadIdx.x * VG;
+            unsigned int* mcol = reinterpret_cast<unsigned int*>(s_acc + (size_t)k * D * NT) + threadIdx.x;
+#pragma unroll
+            for (int i = 0; i < PPT; ++i) {
+                const uint32_t l = T.lab[i];
+                if (p0 + i < n && l < k) {
+                    float* srow = srow0 + (size_t)l * G * NT * VG;
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        float* v = srow + (size_t)g * NT * VG;
+                        if constexpr (VG == 4) {
+                            float4 q = *reinterpret_cast<float4*>(v);
+                            float2 lo = add2(make_float2(q.x, q.y), make_float2(T.x[4 * g][i], T.x[4 * g + 1][i]));
+                            float2 hi = add2(make_float2(q.z, q.w), make_float2(T.x[4 * g + 2][i], T.x[4 * g + 3][i]));
+                            *reinterpret_cast<float4*>(v) = make_float4(lo.x, lo.y, hi.x, hi.y);
+                        } else if constexpr (VG == 2) {
+                            float2 q = *reinterpret_cast<float2*>(v);
+                            *reinterpret_cast<float2*>(v) = add2(q, make_float2(T.x[2 * g][i], T.x[2 * g + 1][i]));
+                        } else {
+                            *v += T.x[g][i];
+                        }
+                    }
+                    mcol[(size_t)l * NT] += 1u;
+                }
+            }
+        } else if constexpr (ACC == 0 || ACC == 2) {
+            // private column per thread: no other thread touches it
             float* col = s_acc + threadIdx.x;
 #pragma unroll
             for (int i = 0; i < PPT; ++i) {
                 const uint32_t l = T.lab[i];
                 if (p0 + i < n && l < k) {
-                    float* row = col + (size_t)l * ((D + 1) * BLK);
+                    float* row = col + (size_t)l * ((D + 1) * NT);
+                    if constexpr (ACC == 0) {
 #pragma unroll
-                    for (int f = 0; f < D; ++f) row[f * BLK] += T.x[f][i];
-                    reinterpret_cast<unsigned int*>(row)[D * BLK] += 1u;
+                        for (int f = 0; f < D; ++f) row[f * NT] += T.x[f][i];
+                        reinterpret_cast<unsigned int*>(row)[D * NT] += 1u;
+                    } else {
+#pragma unroll
+                        for (int f = 0; f < D; ++f) atomicAdd(row + f * NT, T.x[f][i]);
+                        atomicAdd(reinterpret_cast<unsigned int*>(row) + D * NT, 1u);
+                    }
                 }
             }
         } else {
@@ -175,17 +217,17 @@ __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a,
     }
 }
 
-template <int D, int PPT, int ACC, Pass PASS>
-__global__ void __launch_bounds__(BLK, 2)
+template <int D, int PPT, int ACC, Pass PASS, int NT, int MINB, bool PREF>
+__global__ void __launch_bounds__(NT, MINB)
     lowd_kernel(const FusedF32 a, const int vec_ok, const uint64_t ntiles) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t k = a.k;
-    constexpr int W = (ACC == 0) ? BLK : 32;
+    constexpr int W = (ACC == 1) ? 32 : NT;
     float2* s_c = reinterpret_cast<float2*>(smem);
     float* s_acc = reinterpret_cast<float*>(smem + (((size_t)k * D * sizeof(float2) + 15) & ~size_t(15)));
 
     if constexpr (PASS != Pass::SumsOnly) {
-        for (uint32_t i = threadIdx.x; i < k * D; i += BLK) {
+        for (uint32_t i = threadIdx.x; i < k * D; i += NT) {
             const uint32_t c = i / D, f = i - c * D;
             const float v = a.centroids[(size_t)f * k + c];
             s_c[i] = make_float2(v, v);
@@ -193,24 +235,34 @@ __global__ void __launch_bounds__(BLK, 2)
     }
     if constexpr (PASS != Pass::LabelOnly) {
         const uint32_t words = k * (D + 1) * W;
-        for (uint32_t i = threadIdx.x; i < words; i += BLK) s_acc[i] = 0.0f;
+        for (uint32_t i = threadIdx.x; i < words; i += NT) s_acc[i] = 0.0f;
     }
     __syncthreads();
 
     const bool vec = vec_ok != 0;
-    constexpr uint64_t TILE = (uint64_t)BLK * PPT;
-    Tile<D, PPT> A, B;
-    uint64_t t = blockIdx.x;
-    if (t < ntiles) load_tile<D, PPT, PASS>(A, a, t * TILE + threadIdx.x * PPT, vec);
-    while (t < ntiles) {
-        const uint64_t t1 = t + gridDim.x;
-        if (t1 < ntiles) load_tile<D, PPT, PASS>(B, a, t1 * TILE + threadIdx.x * PPT, vec);
-        process_tile<D, PPT, ACC, PASS>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
-        if (t1 >= ntiles) break;
-        const uint64_t t2 = t1 + gridDim.x;
-        if (t2 < ntiles) load_tile<D, PPT, PASS>(A, a, t2 * TILE + threadIdx.x * PPT, vec);
-        process_tile<D, PPT, ACC, PASS>(B, a, t1 * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
-        t = t2;
+    constexpr uint64_t TILE = (uint64_t)NT * PPT;
+    if constexpr (PREF) {
+        // two tiles in flight per thread: the next tile's loads are issued
+        // before the current tile is processed
+        Tile<D, PPT> A, B;
+        uint64_t t = blockIdx.x;
+        if (t < ntiles) load_tile<D, PPT, PASS>(A, a, t * TILE + threadIdx.x * PPT, vec);
+        while (t < ntiles) {
+            const uint64_t t1 = t + gridDim.x;
+            if (t1 < ntiles) load_tile<D, PPT, PASS>(B, a, t1 * TILE + threadIdx.x * PPT, vec);
+            process_tile<D, PPT, ACC, PASS, NT>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
+            if (t1 >= ntiles) break;
+            const uint64_t t2 = t1 + gridDim.x;
+            if (t2 < ntiles) load_tile<D, PPT, PASS>(A, a, t2 * TILE + threadIdx.x * PPT, vec);
+            process_tile<D, PPT, ACC, PASS, NT>(B, a, t1 * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
+            t = t2;
+        }
+    } else {
+        for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            Tile<D, PPT> A;
+            load_tile<D, PPT, PASS>(A, a, t * TILE + threadIdx.x * PPT, vec);
+            process_tile<D, PPT, ACC, PASS, NT>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
+        }
     }
 
     if constexpr (PASS == Pass::LabelOnly) {
@@ -219,8 +271,28 @@ __global__ void __launch_bounds__(BLK, 2)
         __syncthreads();
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         const uint32_t entries = k * (D + 1);
-        for (uint32_t e = warp; e < entries; e += BLK / 32) {
+        for (uint32_t e = warp; e < entries; e += NT / 32) {
             const uint32_t c = e / (D + 1), f = e - c * (D + 1);
+            if constexpr (ACC == 3) {
+                constexpr int VG = AccVec<D>::VG;
+                constexpr int G = D / VG;
+                if (f < D) {
+                    const float* src = s_acc + ((size_t)(c * G + f / VG) * NT) * VG + (f % VG);
+                    float v = 0.0f;
+#pragma unroll 4
+                    for (int j = lane; j < NT; j += 32) v += src[(size_t)j * VG];
+                    v = warp_sum_f32(v);
+                    if (lane == 0 && v != 0.0f) atomicAdd(&a.scratch.sums[(size_t)f * k + c], (double)v);
+                } else {
+                    const unsigned int* usrc = reinterpret_cast<const unsigned int*>(s_acc + (size_t)k * D * NT) + (size_t)c * NT;
+                    unsigned int v = 0;
+#pragma unroll 4
+                    for (int j = lane; j < NT; j += 32) v += usrc[j];
+                    v = __reduce_add_sync(0xffffffffu, v);
+                    if (lane == 0 && v != 0u) atomicAdd(&a.scratch.masses[c], (unsigned long long)v);
+                }
+                continue;
+            }
             const float* src = s_acc + (size_t)e * W;
             if (f < D) {
                 float v = 0.0f;
@@ -242,38 +314,37 @@ __global__ void __launch_bounds__(BLK, 2)
     }
 }
 
-size_t lowd_smem_bytes(uint32_t d, uint32_t k, int acc, Pass pass) {
+size_t lowd_smem_bytes(uint32_t d, uint32_t k, int acc, Pass pass, int nt) {
     size_t b = (((size_t)k * d * sizeof(float2)) + 15) & ~size_t(15);
-    if (pass != Pass::LabelOnly) b += (size_t)k * (d + 1) * (acc == 0 ? BLK : 32) * sizeof(float);
+    if (pass != Pass::LabelOnly) b += (size_t)k * (d + 1) * (acc == 1 ? 32 : nt) * sizeof(float);
     return b;
 }
 
-constexpr size_t PRIVATE_TABLE_LIMIT = 100 * 1024;  // keeps two CTAs per SM
+constexpr size_t PRIVATE_TABLE_LIMIT = 100 * 1024;  // keeps two 256-thread CTAs per SM
 constexpr size_t SHARED_TABLE_LIMIT = 200 * 1024;
 
 int choose_acc(uint32_t d, uint32_t k, Pass pass) {
     if (pass == Pass::LabelOnly) return 0;
-    if (lowd_smem_bytes(d, k, 0, pass) <= PRIVATE_TABLE_LIMIT) return 0;
-    if (lowd_smem_bytes(d, k, 1, pass) <= SHARED_TABLE_LIMIT) return 1;
+    if (lowd_smem_bytes(d, k, 0, pass, BLK) <= PRIVATE_TABLE_LIMIT) return 0;
+    if (lowd_smem_bytes(d, k, 1, pass, BLK) <= SHARED_TABLE_LIMIT) return 1;
     return -1;
 }
 
 struct LaunchCache {
     std::mutex mu;
-    std::unordered_map<const void*, int> attr_set;                 // kernel -> max dyn smem set
-    std::unordered_map<uint64_t, int> occ;                          // (kernel, smem) -> blocks/SM
+    std::unordered_map<const void*, int> attr_set;  // kernel -> max dynamic smem set
+    std::unordered_map<uint64_t, int> occ;          // (kernel, smem) -> blocks per SM
 };
 LaunchCache& cache() {
     static LaunchCache c;
     return c;
 }
 
-template <int D, int ACC, Pass PASS>
-int launch_lowd_t(const FusedF32& a, cudaStream_t s) {
-    constexpr int PPT = LowdCfg<D>::PPT;
-    constexpr int VW = LowdCfg<D>::VW;
-    auto kern = lowd_kernel<D, PPT, ACC, PASS>;
-    const size_t smem = lowd_smem_bytes(D, a.k, ACC, PASS);
+template <int D, int PPT, int ACC, Pass PASS, int NT, int MINB, bool PREF>
+int launch_lowd_v(const FusedF32& a, cudaStream_t s) {
+    constexpr int VW = PPT < 4 ? PPT : 4;
+    auto kern = lowd_kernel<D, PPT, ACC, PASS, NT, MINB, PREF>;
+    const size_t smem = lowd_smem_bytes(D, a.k, ACC, PASS, NT);
     const DeviceInfo& di = device_info();
     if (smem > di.smem_optin) return fail(CKM_ERR_UNSUPPORTED, "lowd: shared-memory table too large");
     int blocks_per_sm = 0;
@@ -296,7 +367,7 @@ int launch_lowd_t(const FusedF32& a, cudaStream_t s) {
         const uint64_t okey = (reinterpret_cast<uint64_t>(key) << 20) ^ (uint64_t)smem;
         auto oi = C.occ.find(okey);
         if (oi == C.occ.end()) {
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, BLK, smem);
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, NT, smem);
             if (e != cudaSuccess) return cuda_fail(e, "occupancy(lowd)");
             if (blocks_per_sm < 1) return fail(CKM_ERR_UNSUPPORTED, "lowd: kernel does not fit on an SM");
             C.occ[okey] = blocks_per_sm;
@@ -304,7 +375,7 @@ int launch_lowd_t(const FusedF32& a, cudaStream_t s) {
             blocks_per_sm = oi->second;
         }
     }
-    const uint64_t tile = (uint64_t)BLK * PPT;
+    const uint64_t tile = (uint64_t)NT * PPT;
     const uint64_t ntiles = (a.n + tile - 1) / tile;
     uint64_t grid = (uint64_t)di.sm_count * (uint64_t)blocks_per_sm;
     if (ntiles < grid) grid = ntiles;
@@ -312,18 +383,52 @@ int launch_lowd_t(const FusedF32& a, cudaStream_t s) {
     const uintptr_t pa = reinterpret_cast<uintptr_t>(a.points);
     const uintptr_t la = reinterpret_cast<uintptr_t>(a.labels);
     const int vec_ok = (a.n % VW == 0) && (pa % (VW * 4) == 0) && (la % (VW * 4) == 0);
-    kern<<<(unsigned)grid, BLK, smem, s>>>(a, vec_ok, ntiles);
+    kern<<<(unsigned)grid, NT, smem, s>>>(a, vec_ok, ntiles);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "lowd launch");
     return CKM_OK;
 }
 
+// Tuning variants of the d = 4 fused pass, selected with the environment
+// variable CKM_LOWD_VARIANT (default 0).  All variants compute the same
+// result; they differ in points per thread, block size, prefetching and the
+// accumulation table (0: private RMW, 1: lane columns shared by the CTA's
+// warps with atomics, 2: private columns with atomic adds).
+int lowd_variant() {
+    static int v = [] {
+        const char* e = getenv("CKM_LOWD_VARIANT");
+        return e ? atoi(e) : 0;
+    }();
+    return v;
+}
+
+int launch_d4_fused_variant(const FusedF32& a, cudaStream_t s, int v) {
+    const size_t priv256 = lowd_smem_bytes(4, a.k, 0, Pass::Fused, 256);
+    const size_t priv128 = lowd_smem_bytes(4, a.k, 0, Pass::Fused, 128);
+    const size_t shared = lowd_smem_bytes(4, a.k, 1, Pass::Fused, 128);
+    switch (v) {
+        case 7: if (priv128 <= PRIVATE_TABLE_LIMIT / 2) return launch_lowd_v<4, 8, 0, Pass::Fused, 128, 4, true>(a, s); break;
+        case 9: if (priv256 <= PRIVATE_TABLE_LIMIT) return launch_lowd_v<4, 8, 0, Pass::Fused, 256, 2, true>(a, s); break;
+        case 10: if (priv256 <= PRIVATE_TABLE_LIMIT) return launch_lowd_v<4, 8, 3, Pass::Fused, 256, 2, false>(a, s); break;
+        default: break;
+    }
+    return -1000;  // not applicable: use the default
+}
+
 template <int D, Pass PASS>
 int launch_lowd_acc(const FusedF32& a, cudaStream_t s) {
+    constexpr int PPT = LowdCfg<D>::PPT;
+    if constexpr (D == 4 && PASS == Pass::Fused) {
+        const int v = lowd_variant();
+        if (v != 0) {
+            int st = launch_d4_fused_variant(a, s, v);
+            if (st != -1000) return st;
+        }
+    }
     const int acc = choose_acc(D, a.k, PASS);
-    if (acc == 0) return launch_lowd_t<D, 0, PASS>(a, s);
-    if (acc == 1) return launch_lowd_t<D, 1, PASS>(a, s);
+    if (acc == 0) return launch_lowd_v<D, PPT, 0, PASS, BLK, 2, false>(a, s);
+    if (acc == 1) return launch_lowd_v<D, PPT, 1, PASS, BLK, 2, true>(a, s);
     return fail(CKM_ERR_UNSUPPORTED, "lowd: no accumulation layout fits");
 }
 
