@@ -31,7 +31,7 @@ STATUS = {
 EXPORTS = [
     "ckm_status_string", "ckm_last_error", "ckm_version", "ckm_device_count", "ckm_launch_count",
     "ckm_scratch_bytes", "ckm_scratch_init",
-    "ckm_fused_f32", "ckm_fused_f64", "ckm_labeling_f32", "ckm_labeling_f64",
+    "ckm_fused_f32", "ckm_fused_f64", "ckm_fused_f32_noalloc", "ckm_labeling_f32", "ckm_labeling_f64",
     "ckm_mass_update_u32", "ckm_mass_update_u64", "ckm_centroid_update_f32", "ckm_centroid_update_f64",
     "ckm_matrix_divide_row_f32", "ckm_matrix_divide_row_f64", "ckm_matrix_add_f32", "ckm_matrix_add_f64",
     "ckm_matrix_add_u32", "ckm_matrix_add_u64", "ckm_reduce_vector_parcol_u32",
@@ -105,6 +105,7 @@ def lib():
         "ckm_scratch_init": ([vp, sz, vp], i32),
         "ckm_fused_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
         "ckm_fused_f64": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
+        "ckm_fused_f32_noalloc": ([u32, u64, u32, vp, vp, vp, vp, vp, i32, vp], i32),
         "ckm_labeling_f32": ([u32, u64, u32, vp, vp, vp, vp], i32),
         "ckm_labeling_f64": ([u32, u64, u32, vp, vp, vp, vp], i32),
         "ckm_mass_update_u32": ([u64, u32, vp, vp, vp], i32),
@@ -178,6 +179,14 @@ def fused(points, old_centroids, new_centroids, labels, masses, scratch, n, d, k
     fn = lib().ckm_fused_f64 if _is64(points) else lib().ckm_fused_f32
     check(fn(d, n, k, _p(points), _p(old_centroids), _p(new_centroids), _p(labels), _p(masses), _p(scratch),
              scratch.numel(), mode, _stream(stream)), "ckm_fused")
+
+
+def fused_noalloc(points, old_centroids, new_centroids, labels, masses, n, d, k, mode=MODE_FINALIZE,
+                  stream=None):
+    """ckm_fused_f32_noalloc: the fused iteration with the library's built-in
+    scratch, for callers that cannot allocate (no scratch argument)."""
+    check(lib().ckm_fused_f32_noalloc(d, n, k, _p(points), _p(old_centroids), _p(new_centroids), _p(labels),
+                                      _p(masses), mode, _stream(stream)), "ckm_fused_f32_noalloc")
 
 
 def labeling(points, centroids, labels, n, d, k, stream=None):

@@ -105,6 +105,22 @@ int ckm_fused_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clust
                   uint64_t *labels, uint64_t *masses, void *scratch, size_t scratch_bytes,
                   int mode, ckm_stream_t stream);
 
+/* The same fused iteration for callers that cannot allocate device memory
+ * (a plugin inside a framework that owns all device memory, a loop that
+ * must never call cudaMalloc/cudaFree, a caller given only its buffers).
+ * No counterpart in the reference: its functors allocate their own partial
+ * buffers.  The FP64 merge scratch is a built-in 128 KiB device array
+ * instead of an argument, which caps ckm_scratch_bytes(d, k) at 128 KiB
+ * (about k*d <= 15,000; larger sizes return CKM_ERR_SCRATCH_TOO_SMALL).
+ * mode: CKM_MODE_FINALIZE or CKM_MODE_ACCUMULATE.  The array is shared by
+ * all calls on a device: calls that may overlap on the GPU race, so keep
+ * them on one stream.  Each call clears the part it uses first.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress);
+ * make it before any stream capture. */
+int ckm_fused_f32_noalloc(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                          const float *points, const float *old_centroids, float *new_centroids,
+                          uint32_t *labels, uint32_t *masses, int mode, ckm_stream_t stream);
+
 /* Labels only.  Replaces LabelingFactory::LabelingFunction
  * (labeling_factory.hpp:33-48) = LabelingUnrollVector::operator()
  * (cl_kernels/labeling_unroll_vector.hpp:168-272). */
