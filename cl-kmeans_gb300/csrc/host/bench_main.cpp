@@ -77,6 +77,10 @@ public:
                 csv_file_ = take("--csv");
             } else if (key == "--config") {
                 config_file_ = take("--config");
+            } else if (key == "--print-config") {
+                print_config_ = true;
+            } else if (key == "--info") {
+                info_ = true;
             } else if (key == "--generate") {
                 generate_ = take("--generate");
             } else if (key == "--points") {
@@ -108,10 +112,26 @@ public:
                          "  --csv arg             Output measurements to CSV file\n"
                          "  --config arg          Configuration file\n"
                          "  --generate OUT        Write a seeded mixture file (--points --features --blobs\n"
-                         "                        --seed --sigma-lo --sigma-hi)\n";
+                         "                        --seed --sigma-lo --sigma-hi)\n"
+                         "  --print-config        Print the parsed configuration (one key=value per line)\n"
+                         "  --info                Print the header of the input file\n";
             return -1;
         }
         if (!generate_.empty()) return 1;
+        if (info_) {
+            if (input_file_.empty()) {
+                std::cout << "No input file specified." << std::endl;
+                return -1;
+            }
+            return 1;
+        }
+        if (print_config_) {
+            if (config_file_.empty()) {
+                std::cout << "No config file specified." << std::endl;
+                return -1;
+            }
+            return 1;
+        }
         if (input_file_.empty()) {
             std::cout << "No input file specified." << std::endl;
             return -1;
@@ -123,7 +143,7 @@ public:
         return 1;
     }
 
-    bool help_ = false, verbose_ = false, verify_ = false;
+    bool help_ = false, verbose_ = false, verify_ = false, print_config_ = false, info_ = false;
     uint32_t k_ = 0, runs_ = 0, iterations_ = 0;
     std::string input_file_, csv_file_, config_file_, generate_;
     uint64_t gen_points_ = 1 << 20, gen_seed_ = 42;
@@ -362,6 +382,61 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
     return 1;
 }
 
+void print_sizes(const char* key, const size_t v[3]) {
+    std::cout << key << "=" << v[0] << "," << v[1] << "," << v[2] << "\n";
+}
+
+// Prints every field of the parsed configuration structs, one key=value per
+// line, in the .conf key names (unset fields show their defaults).
+int print_config(const ConfigurationParser& c) {
+    auto b = c.get_benchmark_configuration();
+    auto k = c.get_kmeans_configuration();
+    auto l = c.get_labeling_configuration();
+    auto m = c.get_mass_update_configuration();
+    auto u = c.get_centroid_update_configuration();
+    auto f = c.get_fused_configuration();
+    auto g = c.get_gb300_configuration();
+    std::cout << "benchmark.runs=" << b.runs << "\nbenchmark.verify=" << b.verify << "\n";
+    std::cout << "kmeans.clusters=" << k.clusters << "\nkmeans.pipeline=" << k.pipeline
+              << "\nkmeans.iterations=" << k.iterations << "\nkmeans.converge=" << k.converge
+              << "\nkmeans.types.point=" << k.point_type << "\nkmeans.types.label=" << k.label_type
+              << "\nkmeans.types.mass=" << k.mass_type << "\n";
+    std::cout << "kmeans.labeling.platform=" << l.platform << "\nkmeans.labeling.device=" << l.device
+              << "\nkmeans.labeling.strategy=" << l.strategy << "\n";
+    print_sizes("kmeans.labeling.global_size", l.global_size);
+    print_sizes("kmeans.labeling.local_size", l.local_size);
+    std::cout << "kmeans.labeling.vector_length=" << l.vector_length
+              << "\nkmeans.labeling.unroll_clusters_length=" << l.unroll_clusters_length
+              << "\nkmeans.labeling.unroll_features_length=" << l.unroll_features_length << "\n";
+    std::cout << "kmeans.mass_update.platform=" << m.platform << "\nkmeans.mass_update.device=" << m.device
+              << "\nkmeans.mass_update.strategy=" << m.strategy << "\n";
+    print_sizes("kmeans.mass_update.global_size", m.global_size);
+    print_sizes("kmeans.mass_update.local_size", m.local_size);
+    std::cout << "kmeans.mass_update.vector_length=" << m.vector_length << "\n";
+    std::cout << "kmeans.centroid_update.platform=" << u.platform << "\nkmeans.centroid_update.device=" << u.device
+              << "\nkmeans.centroid_update.strategy=" << u.strategy << "\n";
+    print_sizes("kmeans.centroid_update.global_size", u.global_size);
+    print_sizes("kmeans.centroid_update.local_size", u.local_size);
+    std::cout << "kmeans.centroid_update.local_features=" << u.local_features
+              << "\nkmeans.centroid_update.thread_features=" << u.thread_features
+              << "\nkmeans.centroid_update.vector_length=" << u.vector_length << "\n";
+    std::cout << "kmeans.fused.platform=" << f.platform << "\nkmeans.fused.device=" << f.device
+              << "\nkmeans.fused.strategy=" << f.strategy << "\n";
+    print_sizes("kmeans.fused.global_size", f.global_size);
+    print_sizes("kmeans.fused.local_size", f.local_size);
+    std::cout << "kmeans.fused.vector_length=" << f.vector_length << "\n";
+    std::cout << "kmeans.gb300.device_budget_mib=" << g.device_budget_mib << "\nkmeans.gb300.chunk_mib=" << g.chunk_mib
+              << "\nkmeans.gb300.copy_streams=" << g.copy_streams << "\nkmeans.gb300.graphs=" << g.graphs << "\n";
+    return 1;
+}
+
+int file_info(const std::string& path) {
+    BinaryHeader h = BinaryFormat::read_header(path);
+    std::cout << "num_features=" << h.num_features << "\nnum_clusters=" << h.num_clusters
+              << "\nnum_points=" << h.num_points << "\n";
+    return 1;
+}
+
 int generate(const CmdOptions& opt) {
     const uint64_t n = opt.gen_points_, d = opt.gen_features_;
     std::vector<float> host(n * d);
@@ -388,8 +463,10 @@ int main(int argc, char** argv) {
         CmdOptions options;
         if (options.parse(argc, argv) < 0) return options.help_ ? 0 : 1;
         if (!options.generate_.empty()) return generate(options) > 0 ? 0 : 1;
+        if (options.info_) return file_info(options.input_file_) > 0 ? 0 : 1;
         ConfigurationParser config;
         config.parse_file(options.config_file_);
+        if (options.print_config_) return print_config(config) > 0 ? 0 : 1;
         auto km = config.get_kmeans_configuration();
         if (km.point_type == "double" && km.label_type == "uint64" && km.mass_type == "uint64")
             return run_bench<double, uint64_t, uint64_t>(options, config) > 0 ? 0 : 1;
