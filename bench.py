@@ -200,13 +200,119 @@ def run_reference_arm(args, workload):
     return 0
 
 
+def make_batched_jobs(ckm, torch, num_jobs, seed_base, dev):
+    """Batched-jobs workload: per job n log-uniform in [2^10, 2^18], d from
+    {2, 8, 32, 64}, k log-uniform in [4, 256] with k <= n/16, its own mixture
+    of k blobs (centres U[-10,10]^d, sigma 1) from seed base + job id,
+    initial centroids = first k points."""
+    rng = np.random.default_rng(seed_base)
+    jobs = []
+    for j in range(num_jobs):
+        n = int(round(np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 18)))))
+        d = int(rng.choice([2, 8, 32, 64]))
+        k = int(round(np.exp(rng.uniform(np.log(4), np.log(256)))))
+        k = max(1, min(k, n // 16))
+        P = torch.empty(n * d, dtype=torch.float32, device=dev)
+        ckm.generate_mixture(P, n, d, k, seed_base + j, sigma=(1.0, 1.0))
+        C0 = P.view(d, n)[:, :k].reshape(-1).clone()
+        jobs.append(dict(points=P, centroids=C0.clone(), init=C0,
+                         labels=torch.empty(n, dtype=torch.int32, device=dev),
+                         masses=torch.empty(k, dtype=torch.int32, device=dev), n=n, d=d, k=k))
+    return jobs
+
+
+def run_batched_workload(args, ckm, torch, dev):
+    """Batched uneven jobs: every job 20 fixed iterations, all jobs advanced by
+    one persistent launch per iteration (CUDA graph), against the plain
+    per-job loop (each job: its own fused launch per iteration) on the same
+    GPU.  Metric: jobs/s."""
+    num_jobs, iters = args.jobs, 20
+    jobs = make_batched_jobs(ckm, torch, num_jobs, 1234, dev)
+    total_pts = sum(j["n"] for j in jobs)
+    stream = torch.cuda.current_stream()
+
+    # plain per-job loop (the reference's one-problem-at-a-time structure)
+    scratch = {}
+    alt = [torch.empty_like(j["centroids"]) for j in jobs]
+
+    def plain_all():
+        for j, a in zip(jobs, alt):
+            key = (j["d"], j["k"])
+            if key not in scratch:
+                scratch[key] = ckm.new_scratch(j["d"], j["k"], dev)
+            bufs = [j["centroids"], a]
+            for it in range(iters):
+                ckm.fused(j["points"], bufs[it % 2], bufs[(it + 1) % 2], j["labels"], j["masses"], scratch[key],
+                          j["n"], j["d"], j["k"], ckm.MODE_FINALIZE, stream)
+
+    for j in jobs:
+        j["centroids"].copy_(j["init"])
+    plain_all()  # warm-up (also allocates scratch)
+    for j in jobs:
+        j["centroids"].copy_(j["init"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_all()
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_result = [(a if iters % 2 else j["centroids"]).clone() for j, a in zip(jobs, alt)]
+
+    # batched: one persistent launch per iteration, captured in a graph
+    for j in jobs:
+        j["centroids"].copy_(j["init"])
+    batch = ckm.Batch(jobs, autotune=True)
+    info = batch.info()
+    for j in jobs:
+        j["centroids"].copy_(j["init"])
+    batch.run(iters, use_graph=True)      # capture + warm-up
+    times = []
+    for _ in range(max(3, args.steps if args.steps < 20 else 5)):
+        for j in jobs:
+            j["centroids"].copy_(j["init"])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches0 = ckm.launch_count()
+        e0.record(stream)
+        batch.run(iters, use_graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        gpu_launches = ckm.launch_count() - launches0
+    batch_s = statistics.median(times)
+    # agreement with the plain loop (same arithmetic; FP64-merged sums)
+    worst = 0.0
+    for j, ref in zip(jobs, plain_result):
+        a, b = j["centroids"].cpu().numpy(), ref.cpu().numpy()
+        ok = ~(np.isnan(a) | np.isnan(b))
+        if ok.any():
+            scale = max(float(np.abs(b[ok]).max()), 1e-30)
+            worst = max(worst, float(np.abs(a[ok] - b[ok]).max()) / scale)
+    batch.close()
+    line = {
+        "metric": "jobs/s", "value": num_jobs / batch_s, "unit": "jobs/s", "n_gpus": 1, "steps": len(times),
+        "warmup": 1, "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (per-job seeded Gaussian mixtures generated on the device)",
+        "config": {"workload": "batched_%d_jobs" % num_jobs, "iterations": iters, "total_points": total_pts,
+                   "schedule": info, "graph": True},
+        "plain_per_job_loop": {"jobs_per_s": num_jobs / plain_s, "seconds": plain_s,
+                               "launches": num_jobs * iters},
+        "speedup_vs_plain_loop": plain_s / batch_s,
+        "pts_iter_per_s": total_pts * iters / batch_s,
+        "max_rel_centroid_diff_vs_plain_loop": worst,
+        "gpu_launches": int(gpu_launches),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched"])
+    ap.add_argument("--jobs", type=int, default=4096, help="batched workload: number of jobs")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -215,6 +321,13 @@ def main():
 
     if args.impl == "reference":
         return run_reference_arm(args, workload)
+
+    if workload == "batched":
+        import importlib
+
+        import torch
+        ckm = importlib.import_module("cl-kmeans_gb300")
+        return run_batched_workload(args, ckm, torch, torch.device("cuda", 0))
 
     import importlib
 

@@ -255,3 +255,111 @@ def kmeans_run(points, d, k, iterations, centroids, pipeline="single_stage", fus
     check(fn(ctypes.byref(cfg), iterations, d, n, k, P.ctypes.data, C.ctypes.data, M.ctypes.data,
              Lb.ctypes.data, ctypes.byref(info)), "ckm_kmeans_run")
     return C, M, Lb, info
+
+
+# ----------------------------------------------------------------------------
+# Batched jobs (ckm_batch_*)
+# ----------------------------------------------------------------------------
+class BatchJob(ctypes.Structure):
+    """struct ckm_batch_job (include/ckm.h)."""
+    _fields_ = [
+        ("points", ctypes.c_void_p),
+        ("centroids", ctypes.c_void_p),
+        ("labels", ctypes.c_void_p),
+        ("masses", ctypes.c_void_p),
+        ("num_points", ctypes.c_uint64),
+        ("num_features", ctypes.c_uint32),
+        ("num_clusters", ctypes.c_uint32),
+    ]
+
+
+class BatchOptions(ctypes.Structure):
+    """struct ckm_batch_options (include/ckm.h)."""
+    _fields_ = [
+        ("tile_points", ctypes.c_uint32),
+        ("ctas_per_sm", ctypes.c_uint32),
+        ("flush_tiles", ctypes.c_uint32),
+        ("autotune", ctypes.c_int),
+    ]
+
+
+_BATCH_SIGS = {
+    "ckm_batch_create": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                          ctypes.c_void_p], ctypes.c_int),
+    "ckm_batch_step": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ckm_batch_run": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "ckm_batch_sync": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ckm_batch_status": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ckm_batch_set_active": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ckm_batch_info": ([ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_uint32)] * 4, ctypes.c_int),
+    "ckm_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
+}
+EXPORTS += list(_BATCH_SIGS)
+
+
+def _batch_lib():
+    L = lib()
+    if not getattr(L, "_batch_sigs", False):
+        for name, (args, res) in _BATCH_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        L._batch_sigs = True
+    return L
+
+
+class Batch:
+    """Owns a ckm_batch handle over torch device tensors (per job: points,
+    centroids, labels, masses).  The tensors must outlive the batch."""
+
+    def __init__(self, jobs, tile_points=0, ctas_per_sm=0, flush_tiles=0, autotune=False, stream=None):
+        L = _batch_lib()
+        self._keep = jobs
+        arr = (BatchJob * len(jobs))()
+        for i, j in enumerate(jobs):
+            arr[i] = BatchJob(j["points"].data_ptr(), j["centroids"].data_ptr(), j["labels"].data_ptr(),
+                              j["masses"].data_ptr(), j["n"], j["d"], j["k"])
+        opt = BatchOptions(tile_points, ctas_per_sm, flush_tiles, 1 if autotune else 0)
+        h = ctypes.c_void_p()
+        check(L.ckm_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(jobs), ctypes.byref(opt), ctypes.byref(h),
+                                 _stream(stream)), "ckm_batch_create")
+        self.h = h
+        self.n_jobs = len(jobs)
+
+    def step(self, stream=None):
+        check(_batch_lib().ckm_batch_step(self.h, _stream(stream)), "ckm_batch_step")
+
+    def run(self, iterations, use_graph=True, stream=None):
+        check(_batch_lib().ckm_batch_run(self.h, iterations, 1 if use_graph else 0, _stream(stream)), "ckm_batch_run")
+
+    def sync(self, stream=None):
+        check(_batch_lib().ckm_batch_sync(self.h, _stream(stream)), "ckm_batch_sync")
+
+    def status(self, stream=None):
+        import numpy as np
+        sh = np.zeros(self.n_jobs, np.float32)
+        it = np.zeros(self.n_jobs, np.uint32)
+        check(_batch_lib().ckm_batch_status(self.h, sh.ctypes.data, it.ctypes.data, _stream(stream)),
+              "ckm_batch_status")
+        return sh, it
+
+    def set_active(self, active, stream=None):
+        import numpy as np
+        a = np.ascontiguousarray(np.asarray(active, np.uint8))
+        check(_batch_lib().ckm_batch_set_active(self.h, a.ctypes.data, _stream(stream)), "ckm_batch_set_active")
+
+    def info(self):
+        v = [ctypes.c_uint32() for _ in range(4)]
+        check(_batch_lib().ckm_batch_info(self.h, *[ctypes.byref(x) for x in v]), "ckm_batch_info")
+        return dict(zip(("grid", "tile_points", "ctas_per_sm", "segments"), (x.value for x in v)))
+
+    def close(self):
+        if self.h:
+            _batch_lib().ckm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

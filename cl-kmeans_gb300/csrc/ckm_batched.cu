@@ -1,0 +1,327 @@
+// Batched Lloyd iterations: many independent k-means jobs of uneven n, d and
+// k in ONE persistent launch per iteration.
+//
+// The host cuts every job into tiles of `tile` points and assigns contiguous
+// runs of tiles ("segments", never spanning two jobs) to the CTAs so that the
+// estimated cost (points x (k*d + overhead)) per CTA is balanced.  A CTA walks
+// its segments; per segment it stages the job's centroids in shared memory,
+// labels each point with the reference's exact arithmetic (fma(t,t,acc) over
+// the features, strict '<' argmin from cluster 0; kmeans_naive.cpp:48-63) and
+// adds it into a shared-memory sum/mass table, which it merges into the job's
+// FP64 scratch every `flush` tiles and at the end of the segment.  Each job
+// carries a tile ticket: the CTA whose merge completes the job's tiles
+// finalises that job (centroids = sums / masses into the other buffer of the
+// job's centroid pair, masses, relative centroid shift) and re-zeroes its
+// scratch.  Nothing waits on another CTA.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ckm_batched.h"
+#include "ckm_device.cuh"
+#include "ckm_internal.h"
+
+namespace ckm {
+
+namespace {
+
+constexpr int BT = 256;  // threads per CTA
+
+// Shared memory per CTA: centroids [c][f] (if they fit) + sum table [f][c] +
+// mass table [c].
+__device__ __forceinline__ void stage_centroids(const BatchJobDev& J, const float* __restrict__ src, float* s_c,
+                                                bool cent_smem) {
+    if (!cent_smem) return;
+    const uint32_t k = J.k, d = J.d;
+    for (uint32_t i = threadIdx.x; i < k * d; i += BT) {
+        const uint32_t c = i / d, f = i - c * d;
+        s_c[i] = src[(size_t)f * k + c];
+    }
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t label_point_fixed(const float (&x)[D], const float* __restrict__ cs, uint32_t k) {
+    float best = FLT_MAX;
+    uint32_t lab = 0;
+    for (uint32_t c = 0; c < k; ++c) {
+        const float* cr = cs + (size_t)c * D;
+        float t = x[0] - cr[0];
+        float acc = t * t;
+#pragma unroll
+        for (int f = 1; f < D; ++f) {
+            t = x[f] - cr[f];
+            acc = fmaf(t, t, acc);
+        }
+        if (acc < best) {
+            best = acc;
+            lab = c;
+        }
+    }
+    return lab;
+}
+
+__device__ __forceinline__ uint32_t label_point_generic(const float* __restrict__ P, uint64_t n, uint64_t p,
+                                                        const float* __restrict__ cs, bool cent_smem,
+                                                        const float* __restrict__ gc, uint32_t k, uint32_t d) {
+    float best = FLT_MAX;
+    uint32_t lab = 0;
+    for (uint32_t c = 0; c < k; ++c) {
+        float acc = 0.f;
+        for (uint32_t f = 0; f < d; ++f) {
+            const float cf = cent_smem ? cs[(size_t)c * d + f] : __ldg(gc + (size_t)f * k + c);
+            const float t = __ldg(P + (size_t)f * n + p) - cf;
+            acc = fmaf(t, t, acc);
+        }
+        if (acc < best) {
+            best = acc;
+            lab = c;
+        }
+    }
+    return lab;
+}
+
+// Labels the points of tiles [t0, t1) of one job and adds them into the
+// shared tables (or, when the tables do not fit, straight into the job's FP64
+// scratch).
+template <int D>
+__device__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
+                                float* s_sum, unsigned int* s_mass, bool acc_smem, int parity) {
+    const uint64_t n = J.n;
+    const uint32_t k = J.k;
+    const float* __restrict__ P = J.points;
+    for (uint64_t p = (uint64_t)t0 * tile + threadIdx.x; p < (uint64_t)t1 * tile && p < n; p += BT) {
+        float x[D];
+#pragma unroll
+        for (int f = 0; f < D; ++f) x[f] = __ldg(P + (size_t)f * n + p);
+        const uint32_t lab = label_point_fixed<D>(x, s_c, k);
+        J.labels[p] = lab;
+        if (acc_smem) {
+#pragma unroll
+            for (int f = 0; f < D; ++f) atomicAdd(&s_sum[(size_t)f * k + lab], x[f]);
+            atomicAdd(&s_mass[lab], 1u);
+        } else {
+#pragma unroll
+            for (int f = 0; f < D; ++f) atomicAdd(&J.sums[(size_t)f * k + lab], (double)x[f]);
+            atomicAdd(&J.msum[lab], 1ull);
+        }
+    }
+    (void)parity;
+}
+
+__device__ void run_tiles_generic(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
+                                  bool cent_smem, float* s_sum, unsigned int* s_mass, bool acc_smem, int parity) {
+    const uint64_t n = J.n;
+    const uint32_t k = J.k, d = J.d;
+    const float* __restrict__ P = J.points;
+    const float* gc = J.cent[parity];
+    for (uint64_t p = (uint64_t)t0 * tile + threadIdx.x; p < (uint64_t)t1 * tile && p < n; p += BT) {
+        const uint32_t lab = label_point_generic(P, n, p, s_c, cent_smem, gc, k, d);
+        J.labels[p] = lab;
+        for (uint32_t f = 0; f < d; ++f) {
+            const float v = __ldg(P + (size_t)f * n + p);
+            if (acc_smem) atomicAdd(&s_sum[(size_t)f * k + lab], v);
+            else atomicAdd(&J.sums[(size_t)f * k + lab], (double)v);
+        }
+        if (acc_smem) atomicAdd(&s_mass[lab], 1u);
+        else atomicAdd(&J.msum[lab], 1ull);
+    }
+}
+
+__device__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s_mass) {
+    const uint32_t k = J.k, d = J.d;
+    for (uint32_t i = threadIdx.x; i < k * d; i += BT) {
+        const float v = s_sum[i];
+        if (v != 0.f) atomicAdd(&J.sums[i], (double)v);
+        s_sum[i] = 0.f;
+    }
+    for (uint32_t c = threadIdx.x; c < k; c += BT) {
+        const unsigned int m = s_mass[c];
+        if (m) atomicAdd(&J.msum[c], (unsigned long long)m);
+        s_mass[c] = 0u;
+    }
+}
+
+// Last CTA of a job: centroids, masses, relative shift; scratch back to zero.
+__device__ void finalize_job(const BatchJobDev& J, int parity) {
+    __shared__ float s_red[BT / 32 * 2];
+    const uint32_t k = J.k, d = J.d;
+    const float* old = J.cent[parity];
+    float* out = J.cent[parity ^ 1];
+    float dmax = 0.f, cmax = 0.f;
+    for (uint32_t e = threadIdx.x; e < k * d; e += BT) {
+        const uint32_t c = e % k;
+        const double s = __ldcg(&J.sums[e]);
+        const double m = (double)__ldcg(&J.msum[c]);
+        const float v = (float)(s / m);
+        const float o = old[e];
+        out[e] = v;
+        dmax = fmaxf(dmax, fabsf(v - o));  // NaN (empty cluster) is ignored by fmaxf
+        cmax = fmaxf(cmax, fabsf(o));
+        J.sums[e] = 0.0;
+    }
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < k; c += BT) {
+        J.masses[c] = (uint32_t)__ldcg(&J.msum[c]);
+        J.msum[c] = 0ull;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        cmax = fmaxf(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_red[threadIdx.x >> 5] = dmax;
+        s_red[BT / 32 + (threadIdx.x >> 5)] = cmax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f;
+        for (int w = 0; w < BT / 32; ++w) {
+            a = fmaxf(a, s_red[w]);
+            b = fmaxf(b, s_red[BT / 32 + w]);
+        }
+        J.status->shift = a / fmaxf(b, 1e-30f);
+        J.status->iterations += 1;
+        J.status->parity = (uint32_t)(parity ^ 1);
+        *J.ticket = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restrict__ jobs,
+                                                     const BatchSegment* __restrict__ segs,
+                                                     const uint32_t* __restrict__ seg_off, uint32_t tile,
+                                                     uint32_t flush_tiles, size_t cent_cap, size_t acc_cap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned int s_last;
+    const uint32_t s0 = seg_off[blockIdx.x], s1 = seg_off[blockIdx.x + 1];
+    for (uint32_t si = s0; si < s1; ++si) {
+        const BatchSegment S = segs[si];
+        const BatchJobDev J = jobs[S.job];
+        // parity and flags were last written by the previous launch (or by the
+        // host before it); within a launch only the job's finalising CTA
+        // changes them, after every segment of the job has read them
+        const BatchStatus st = *J.status;
+        if (st.flags & 1u) continue;  // job inactive this step
+        const int parity = (int)(st.parity & 1u);
+        const uint32_t k = J.k, d = J.d;
+        const size_t cbytes = (size_t)k * d * sizeof(float);
+        const bool cent_smem = cbytes <= cent_cap;
+        const size_t tbytes = ((size_t)k * d + k) * sizeof(float);
+        const bool acc_smem = tbytes <= acc_cap;
+        float* s_c = reinterpret_cast<float*>(smem);
+        float* s_sum = reinterpret_cast<float*>(smem + cent_cap);
+        unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d);
+        __syncthreads();  // previous segment's readers of the shared tables are done
+        stage_centroids(J, J.cent[parity], s_c, cent_smem);
+        if (acc_smem) {
+            for (uint32_t i = threadIdx.x; i < k * d; i += BT) s_sum[i] = 0.f;
+            for (uint32_t c = threadIdx.x; c < k; c += BT) s_mass[c] = 0u;
+        }
+        __syncthreads();
+        for (uint32_t t = S.tile_begin; t < S.tile_end; t += flush_tiles) {
+            const uint32_t te = min(S.tile_end, t + flush_tiles);
+            if (cent_smem) {
+                switch (d) {
+                    case 2: run_tiles_fixed<2>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
+                    case 4: run_tiles_fixed<4>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
+                    case 8: run_tiles_fixed<8>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
+                    case 16: run_tiles_fixed<16>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
+                    case 32: run_tiles_fixed<32>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
+                    case 64: run_tiles_fixed<64>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
+                    default: run_tiles_generic(J, t, te, tile, s_c, true, s_sum, s_mass, acc_smem, parity); break;
+                }
+            } else {
+                run_tiles_generic(J, t, te, tile, s_c, false, s_sum, s_mass, acc_smem, parity);
+            }
+            if (acc_smem) {
+                __syncthreads();
+                flush_tables(J, s_sum, s_mass);
+                __syncthreads();
+            }
+        }
+        // ticket: the CTA that completes the job's tiles finalises it
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t mine = S.tile_end - S.tile_begin;
+            const unsigned int before = atomicAdd(J.ticket, mine);
+            s_last = (before + mine == J.num_tiles) ? 1u : 0u;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            finalize_job(J, parity);
+        }
+    }
+}
+
+// Raises the kernel's dynamic shared-memory limit (once per device) to the
+// opt-in maximum minus its static shared memory.
+int ensure_batched_attr() {
+    static bool attr_done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
+        cudaFuncAttributes fa;
+        cudaError_t e = cudaFuncGetAttributes(&fa, batched_kernel);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(batched)");
+        e = cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(device_info().smem_optin - fa.sharedSizeBytes));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batched)");
+        attr_done[dev] = true;
+    }
+    return CKM_OK;
+}
+
+}  // namespace
+
+int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, const uint32_t* seg_off, uint32_t grid,
+                   uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s) {
+    const size_t smem = cent_cap + acc_cap;
+    int st = ensure_batched_attr();
+    if (st) return st;
+    if (grid == 0) return CKM_OK;
+    batched_kernel<<<grid, BT, smem, s>>>(jobs, segs, seg_off, tile, flush_tiles, cent_cap, acc_cap);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batched launch");
+}
+
+int batched_blocks_per_sm(size_t smem, int* out) {
+    int st = ensure_batched_attr();
+    if (st) return st;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batched_kernel, BT, smem) == cudaSuccess
+               ? CKM_OK
+               : fail(CKM_ERR_CUDA, "occupancy(batched)");
+}
+
+}  // namespace ckm
+
+namespace ckm {
+namespace {
+
+__global__ void batch_sync_kernel(const BatchJobDev* __restrict__ jobs, uint32_t num_jobs) {
+    for (uint32_t j = blockIdx.x; j < num_jobs; j += gridDim.x) {
+        const BatchJobDev J = jobs[j];
+        if ((J.status->parity & 1u) == 0u) continue;
+        const uint32_t kd = J.k * J.d;
+        for (uint32_t i = threadIdx.x; i < kd; i += blockDim.x) J.cent[0][i] = J.cent[1][i];
+        __syncthreads();
+        if (threadIdx.x == 0) J.status->parity = 0u;
+    }
+}
+
+}  // namespace
+
+int launch_batch_sync(const BatchJobDev* jobs, uint32_t num_jobs, cudaStream_t s) {
+    if (num_jobs == 0) return CKM_OK;
+    const uint32_t grid = num_jobs < 4096u ? num_jobs : 4096u;
+    batch_sync_kernel<<<grid, 256, 0, s>>>(jobs, num_jobs);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batch sync launch");
+}
+
+}  // namespace ckm

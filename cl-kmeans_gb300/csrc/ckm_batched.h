@@ -1,0 +1,45 @@
+// Device-side descriptors of the batched Lloyd kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace ckm {
+
+// Per-job state kept on the device between iterations.
+struct BatchStatus {
+    float shift;          // max |new - old| / max |old| of the last iteration
+    uint32_t iterations;  // iterations finished
+    uint32_t parity;      // centroids live in cent[parity]; flipped by the finalising CTA
+    uint32_t flags;       // bit 0: inactive (skipped by the step)
+};
+
+struct BatchJobDev {
+    const float* points;        // column-major n x d
+    float* cent[2];             // centroid double buffer, column-major k x d
+    uint32_t* labels;
+    uint32_t* masses;
+    double* sums;               // FP64 scratch [f * k + c]
+    unsigned long long* msum;   // [k]
+    unsigned int* ticket;       // tiles merged this iteration
+    BatchStatus* status;
+    uint64_t n;
+    uint32_t d, k;
+    uint32_t num_tiles;
+    uint32_t pad;
+};
+
+// A contiguous run of one job's tiles processed by one CTA.
+struct BatchSegment {
+    uint32_t job, tile_begin, tile_end, pad;
+};
+
+int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, const uint32_t* seg_off, uint32_t grid,
+                   uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s);
+int batched_blocks_per_sm(size_t smem, int* out);
+// Copies cent[1] into cent[0] for every job whose parity is 1 and resets the
+// parity, so the caller's centroid arrays hold the current centroids.
+int launch_batch_sync(const BatchJobDev* jobs, uint32_t num_jobs, cudaStream_t s);
+
+}  // namespace ckm

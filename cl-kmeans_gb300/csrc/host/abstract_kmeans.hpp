@@ -86,6 +86,10 @@ public:
 
         auto current = this->measurement;
         this->measurement.reset(new Measurement::Measurement);
+        // strategy parameters (recorded once by the factories) carry over to
+        // the next run's measurement; the reference loses them after run 0
+        for (const auto& p : current->parameters())
+            if (p.first != "TimeStamp") this->measurement->set_parameter(p.first, p.second);
         return current;
     }
 

@@ -200,6 +200,56 @@ int ckm_generate_mixture_f32(uint32_t num_features, uint64_t num_points, uint32_
                              uint64_t points_stride, ckm_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Batched jobs: many independent k-means problems of uneven size advanced  */
+/* by ONE persistent kernel launch per iteration.  No counterpart in the    */
+/* reference (it runs one problem per bench invocation).  The handle owns   */
+/* the device job table, the CTA schedule and every job's FP64 scratch and  */
+/* second centroid buffer, all allocated by ckm_batch_create; stepping      */
+/* allocates nothing.  Each job's arrays are the caller's device arrays.    */
+/* ---------------------------------------------------------------------- */
+typedef struct ckm_batch_job {
+    const float *points;    /* device, column-major num_points x num_features */
+    float *centroids;       /* device, column-major num_clusters x num_features; in: initial */
+    uint32_t *labels;       /* device [num_points], out */
+    uint32_t *masses;       /* device [num_clusters], out */
+    uint64_t num_points;
+    uint32_t num_features;
+    uint32_t num_clusters;
+} ckm_batch_job;
+
+typedef struct ckm_batch_options {
+    uint32_t tile_points;   /* points per tile; 0 = choose (autotune or default) */
+    uint32_t ctas_per_sm;   /* 0 = choose */
+    uint32_t flush_tiles;   /* tiles between FP64 merges of a CTA's partial sums; 0 = 16 */
+    int autotune;           /* time candidate tile sizes / CTA counts on the batch itself */
+} ckm_batch_options;
+
+typedef struct ckm_batch ckm_batch;
+
+/* Uploads the job table and builds a cost-balanced schedule.  jobs may be
+ * freed after the call; the device arrays they point to must stay alive. */
+int ckm_batch_create(const ckm_batch_job *jobs, uint32_t num_jobs, const ckm_batch_options *options,
+                     ckm_batch **out, ckm_stream_t stream);
+/* One Lloyd iteration of every active job: one kernel launch. */
+int ckm_batch_step(ckm_batch *batch, ckm_stream_t stream);
+/* `iterations` steps (captured once into a CUDA graph and replayed when
+ * use_graph != 0), then brings every job's current centroids into its
+ * `centroids` array. */
+int ckm_batch_run(ckm_batch *batch, uint32_t iterations, int use_graph, ckm_stream_t stream);
+/* Brings the current centroids into the jobs' `centroids` arrays. */
+int ckm_batch_sync(ckm_batch *batch, ckm_stream_t stream);
+/* Per-job relative centroid shift of the last step (max |new - old| over
+ * max |old|) and iterations done; host arrays of num_jobs entries (either
+ * may be NULL).  Synchronises the stream. */
+int ckm_batch_status(ckm_batch *batch, float *shifts, uint32_t *iterations, ckm_stream_t stream);
+/* Marks jobs active (1) or inactive (0); inactive jobs are skipped by steps. */
+int ckm_batch_set_active(ckm_batch *batch, const uint8_t *active, ckm_stream_t stream);
+/* Schedule facts: grid, tile points, CTAs per SM, segments. */
+int ckm_batch_info(const ckm_batch *batch, uint32_t *grid, uint32_t *tile_points, uint32_t *ctas_per_sm,
+                   uint32_t *segments);
+int ckm_batch_destroy(ckm_batch *batch);
+
+/* ---------------------------------------------------------------------- */
 /* Host-level run: AbstractKmeans<PointT,LabelT,MassT>::operator()          */
 /* (abstract_kmeans.hpp:106-130) through a C ABI, with HOST buffers.  The   */
 /* pipeline and per-stage strategies take the reference's .conf names.      */

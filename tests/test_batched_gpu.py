@@ -1,0 +1,118 @@
+"""Batched jobs (ckm_batch_*): many independent k-means problems of uneven
+n, d and k advanced by one persistent launch per iteration.  Every job must
+behave exactly like the same job run alone: per iteration (lockstep), each
+job's labels are bit-exact against the oracle's FP32 labeling with that
+iteration's input centroids, masses are exact, centroids are within the
+fused tests' tolerance of the FP64 means."""
+import numpy as np
+import pytest
+
+from conftest import blobs
+from test_fused_gpu import check_centroids
+
+pytestmark = pytest.mark.gpu
+
+
+def make_jobs(cuda, oracle, shapes, seed=0):
+    import torch
+    jobs, host = [], []
+    for i, (n, d, k) in enumerate(shapes):
+        P = blobs(n, d, max(1, min(k, 32)), seed=seed * 1000 + i)
+        C = oracle.first_x_f32(P, n, d, k)
+        jobs.append(dict(points=torch.from_numpy(P).to(cuda), centroids=torch.from_numpy(C).to(cuda),
+                         labels=torch.zeros(max(n, 1), dtype=torch.int32, device=cuda),
+                         masses=torch.zeros(k, dtype=torch.int32, device=cuda), n=n, d=d, k=k))
+        host.append(P)
+    return jobs, host
+
+
+SHAPES = [(1024, 2, 4), (5000, 8, 37), (777, 3, 9), (20000, 32, 64), (3000, 64, 256), (65536, 4, 16),
+          (1031, 5, 7), (100, 16, 6), (12345, 2, 200), (40000, 8, 8), (2048, 64, 64), (1, 2, 1)]
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(tile_points=256, ctas_per_sm=2), dict(tile_points=4096),
+                                  dict(autotune=True)])
+def test_batch_lockstep_matches_oracle(ckm, oracle, cuda, opts):
+    import torch
+    jobs, host = make_jobs(cuda, oracle, SHAPES, seed=1)
+    b = ckm.Batch(jobs, **opts)
+    try:
+        for it in range(4):
+            b.sync()
+            torch.cuda.synchronize()
+            Cin = [j["centroids"].cpu().numpy().copy() for j in jobs]
+            b.step()
+            b.sync()
+            torch.cuda.synchronize()
+            for j, P, C0 in zip(jobs, host, Cin):
+                n, d, k = j["n"], j["d"], j["k"]
+                lab = j["labels"][:n].cpu().numpy().view(np.uint32)
+                ref = oracle.label_f32(P, n, d, k, C0)
+                assert np.array_equal(lab, ref), (it, n, d, k, int((lab != ref).sum()))
+                assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+                check_centroids(oracle, P, n, d, k, ref, j["centroids"].cpu().numpy())
+        sh, its = b.status()
+        assert np.all(its == 4)
+    finally:
+        b.close()
+
+
+def test_batch_graph_run_equals_steps(ckm, oracle, cuda):
+    import torch
+    jobsA, host = make_jobs(cuda, oracle, SHAPES, seed=2)
+    jobsB, _ = make_jobs(cuda, oracle, SHAPES, seed=2)
+    a = ckm.Batch(jobsA, tile_points=1024, ctas_per_sm=1)
+    b = ckm.Batch(jobsB, tile_points=1024, ctas_per_sm=1)
+    try:
+        a.run(6, use_graph=True)
+        for _ in range(6):
+            b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        for ja, jb, P in zip(jobsA, jobsB, host):
+            ca, cb = ja["centroids"].cpu().numpy(), jb["centroids"].cpu().numpy()
+            nan = np.isnan(ca)
+            assert np.array_equal(nan, np.isnan(cb))
+            assert np.allclose(ca[~nan], cb[~nan], rtol=1e-5, atol=1e-4)
+        assert np.all(a.status()[1] == 6)
+        # replaying the cached graph continues from the current state
+        a.run(6, use_graph=True)
+        torch.cuda.synchronize()
+        assert np.all(a.status()[1] == 12)
+    finally:
+        a.close()
+        b.close()
+
+
+def test_batch_inactive_jobs_are_skipped_and_shift_reported(ckm, oracle, cuda):
+    import torch
+    jobs, host = make_jobs(cuda, oracle, SHAPES[:6], seed=3)
+    b = ckm.Batch(jobs)
+    try:
+        active = [1, 0, 1, 0, 1, 1]
+        b.set_active(active)
+        before = [j["centroids"].cpu().numpy().copy() for j in jobs]
+        b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        sh, its = b.status()
+        for i, (j, a, C0) in enumerate(zip(jobs, active, before)):
+            C1 = j["centroids"].cpu().numpy()
+            if not a:
+                assert its[i] == 0 and np.array_equal(C1, C0)
+            else:
+                assert its[i] == 1
+                ok = ~np.isnan(C1)
+                want = np.abs(C1[ok] - C0[ok]).max() / max(np.abs(C0).max(), 1e-30)
+                assert abs(sh[i] - want) <= 1e-6 * max(1.0, want)
+    finally:
+        b.close()
+
+
+def test_batch_rejects_bad_jobs(ckm, cuda):
+    import torch
+    t = torch.zeros(16, dtype=torch.float32, device=cuda)
+    with pytest.raises(ckm.CkmError):
+        ckm.Batch([dict(points=t, centroids=t, labels=t, masses=t, n=4, d=0, k=2)])
+    with pytest.raises(ckm.CkmError):
+        ckm.Batch([])
