@@ -363,3 +363,66 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ----------------------------------------------------------------------------
+# Tensor-core fused iteration (ckm_tc_*)
+# ----------------------------------------------------------------------------
+_TC_SIGS = {
+    "ckm_tc_points_bytes": ([ctypes.c_uint64, ctypes.c_uint32], ctypes.c_size_t),
+    "ckm_tc_workspace_bytes": ([ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_size_t),
+    "ckm_tc_supported": ([ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+    "ckm_tc_prepare_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                               ctypes.c_void_p], ctypes.c_int),
+    "ckm_tc_fused_f32": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32] + [ctypes.c_void_p] * 7 +
+                         [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                          ctypes.c_void_p], ctypes.c_int),
+}
+EXPORTS += list(_TC_SIGS)
+
+
+def _tc_lib():
+    L = lib()
+    if not getattr(L, "_tc_sigs", False):
+        for name, (args, res) in _TC_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        L._tc_sigs = True
+    return L
+
+
+class TensorCorePoints:
+    """A point set prepared for the tensor-core path (bf16 copy + norms) and
+    the per-(n, d, k) workspace; torch device memory."""
+
+    def __init__(self, points, n, d, stream=None):
+        import torch
+        L = _tc_lib()
+        self.n, self.d = n, d
+        nbytes = int(L.ckm_tc_points_bytes(n, d))
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device=points.device)
+        check(L.ckm_tc_prepare_points(d, n, _p(points), _p(self.buf), nbytes, _stream(stream)),
+              "ckm_tc_prepare_points")
+        self.ws = {}
+
+    def workspace(self, k):
+        import torch
+        if k not in self.ws:
+            b = int(_tc_lib().ckm_tc_workspace_bytes(self.n, self.d, k))
+            self.ws[k] = torch.empty(b, dtype=torch.uint8, device=self.buf.device)
+        return self.ws[k]
+
+
+def tc_supported(d, k):
+    return bool(_tc_lib().ckm_tc_supported(d, k))
+
+
+def tc_fused(points, tcp, old_centroids, new_centroids, labels, masses, scratch, n, d, k, mode=MODE_FINALIZE,
+             stats=None, stream=None):
+    """ckm_tc_fused_f32: one Lloyd iteration with tensor-core distances,
+    certified labels and exact recheck of near-ties."""
+    ws = tcp.workspace(k)
+    check(_tc_lib().ckm_tc_fused_f32(d, n, k, _p(points), _p(tcp.buf), _p(old_centroids), _p(new_centroids),
+                                     _p(labels), _p(masses), _p(scratch), scratch.numel(), _p(ws), ws.numel(), mode,
+                                     _p(stats), _stream(stream)), "ckm_tc_fused_f32")
