@@ -305,14 +305,116 @@ def run_batched_workload(args, ckm, torch, dev):
     return 0
 
 
+def measured_bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                j = json.load(f)
+            for key in ("bf16_tflops", "bf16_tflops_burst"):
+                if key in j and j[key]:
+                    return float(j[key]), "measured"
+        except (OSError, ValueError):
+            pass
+    return 1900.0, "fallback"
+
+
+def run_tensor_core_workload(args, ckm, torch, dev):
+    """Tensor-core labeling with precision recovery: n = 2^24, d = 128,
+    k = 1024, a 1024-component mixture (centres ~ N(0, 4 I), sigma
+    log-uniform in [0.25, 1], Dirichlet(1) weights), 20 fixed iterations.
+    One step = one Lloyd iteration via ckm_tc_fused_f32 (bf16 distance GEMM
+    on tcgen05, certified labels, exact FP32 recheck of near-ties, FP64
+    sums)."""
+    n, d, k, iters = 1 << 24, 128, 1024, 20
+    if args.tc_points:
+        n = args.tc_points
+    stream = torch.cuda.current_stream()
+    P = torch.empty(n * d, dtype=torch.float32, device=dev)
+    ckm.generate_mixture_ex(P, n, d, k, SEED, center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0),
+                            dirichlet=True)
+    tcp = ckm.TensorCorePoints(P, n, d)
+    C = [P.view(d, n)[:, :k].reshape(-1).clone(), torch.empty(k * d, dtype=torch.float32, device=dev)]
+    C0 = C[0].clone()
+    L = torch.empty(n, dtype=torch.int32, device=dev)
+    M = torch.empty(k, dtype=torch.int32, device=dev)
+    S = ckm.new_scratch(d, k, dev)
+    stats = torch.zeros(2, dtype=torch.int32, device=dev)
+    steps = min(args.steps, iters)
+    warm = max(3, min(args.warmup, 5))
+    for i in range(warm):
+        ckm.tc_fused(P, tcp, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats, stream)
+    C[0].copy_(C0)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    rechecked = []
+    launches0 = ckm.launch_count()
+    for i in range(steps):
+        evs[i][0].record(stream)
+        ckm.tc_fused(P, tcp, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats, stream)
+        evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        st = stats.cpu().numpy()
+        rechecked.append(int(st[0]))
+        if st[1]:
+            raise RuntimeError("tensor-core kernel reported a timed-out device wait")
+    gpu_launches = ckm.launch_count() - launches0
+    clocks = sampler.stop()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    step_s = statistics.mean(ms) / 1e3
+    flops = 2.0 * n * k * d
+    peak, kind = measured_bf16_peak()
+    achieved = flops / step_s / 1e12
+    # the same iteration on the FP32 SIMT path (exact arithmetic everywhere), one step
+    Ls = torch.empty(n, dtype=torch.int32, device=dev)
+    Cs = torch.empty(k * d, dtype=torch.float32, device=dev)
+    Ss = ckm.new_scratch(d, k, dev)
+    simt_s = None
+    if not args.no_simt_compare:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ckm.fused(P, C0, Cs, Ls, M, Ss, n, d, k, ckm.MODE_FINALIZE, stream)
+        torch.cuda.synchronize()
+        simt_s = time.perf_counter() - t0
+    cpu = None
+    if not args.no_cpu_baseline:
+        n_s = 1 << 12
+        Ps = np.ascontiguousarray(P.view(d, n)[:, :n_s].cpu().numpy()).reshape(-1)
+        rate, dt = cpu_port_rate(Ps, n_s, d, k, 1, 1)
+        cpu = {"value": rate, "unit": "pts*iter/s", "cores": 1, "kind": "port",
+               "sample": "first %d points, 1 iteration, %.1f s" % (n_s, dt)}
+    line = {
+        "metric": "pts*iter/s", "value": n / step_s, "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
+        "warmup": warm, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 distances (tcgen05), f32 recheck, f64 sums",
+        "data": "synthetic (seeded 1024-component mixture generated on the device)",
+        "config": {"workload": "lloyd_tc_n%d_d%d_k%d" % (n, d, k), "n": n, "d": d, "k": k,
+                   "centres": "N(0, 4I)", "sigma": "log-uniform [0.25, 1]", "weights": "Dirichlet(1)",
+                   "l2": "inputs (%.1f GiB) larger than L2, no flush" % (n * d * 6 / 2 ** 30)},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_source": kind, "traffic": None,
+                     "algorithmic_flops_per_step": flops},
+        "rechecked_points_per_step": rechecked,
+        "simt_fp32_step_ms": simt_s * 1e3 if simt_s is not None else None,
+        "cpu_baseline": cpu, "gpu_launches": int(gpu_launches), "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core"])
     ap.add_argument("--jobs", type=int, default=4096, help="batched workload: number of jobs")
+    ap.add_argument("--tc-points", type=int, default=0, help="tensor_core workload: points (default 2^24)")
+    ap.add_argument("--no-simt-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -320,14 +422,15 @@ def main():
     workload = args.workload
 
     if args.impl == "reference":
-        return run_reference_arm(args, workload)
+        return run_reference_arm(args, workload if workload in WORKLOADS else DEFAULT_WORKLOAD)
 
-    if workload == "batched":
+    if workload in ("batched", "tensor_core"):
         import importlib
 
         import torch
         ckm = importlib.import_module("cl-kmeans_gb300")
-        return run_batched_workload(args, ckm, torch, torch.device("cuda", 0))
+        run = run_batched_workload if workload == "batched" else run_tensor_core_workload
+        return run(args, ckm, torch, torch.device("cuda", 0))
 
     import importlib
 

@@ -426,3 +426,32 @@ def tc_fused(points, tcp, old_centroids, new_centroids, labels, masses, scratch,
     check(_tc_lib().ckm_tc_fused_f32(d, n, k, _p(points), _p(tcp.buf), _p(old_centroids), _p(new_centroids),
                                      _p(labels), _p(masses), _p(scratch), scratch.numel(), _p(ws), ws.numel(), mode,
                                      _p(stats), _stream(stream)), "ckm_tc_fused_f32")
+
+
+class MixtureSpec(ctypes.Structure):
+    """struct ckm_mixture_spec (include/ckm.h)."""
+    _fields_ = [
+        ("num_features", ctypes.c_uint32), ("num_blobs", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+        ("center_dist", ctypes.c_int), ("center_a", ctypes.c_float), ("center_b", ctypes.c_float),
+        ("sigma_dist", ctypes.c_int), ("sigma_lo", ctypes.c_float), ("sigma_hi", ctypes.c_float),
+        ("dirichlet", ctypes.c_int),
+    ]
+
+
+EXPORTS.append("ckm_generate_mixture_ex_f32")
+
+
+def generate_mixture_ex(points, n, d, blobs, seed, center=("uniform", -10.0, 10.0), sigma=("uniform", 1.0, 1.0),
+                        dirichlet=False, first_point=0, stride=None, stream=None):
+    """ckm_generate_mixture_ex_f32: centre law 'uniform' (a, b) or 'normal'
+    (mean, std); sigma law 'uniform' or 'loguniform' (lo, hi); equal or
+    Dirichlet(1) weights."""
+    L = lib()
+    fn = L.ckm_generate_mixture_ex_f32
+    fn.argtypes = [ctypes.POINTER(MixtureSpec), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                   ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    spec = MixtureSpec(d, blobs, seed, 1 if center[0] == "normal" else 0, center[1], center[2],
+                       1 if sigma[0] == "loguniform" else 0, sigma[1], sigma[2], 1 if dirichlet else 0)
+    check(fn(ctypes.byref(spec), n, first_point, _p(points), n if stride is None else stride, _stream(stream)),
+          "ckm_generate_mixture_ex_f32")

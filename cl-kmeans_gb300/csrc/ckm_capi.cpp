@@ -97,12 +97,6 @@ int check_shape(uint32_t d, uint64_t n, uint32_t k) {
     return CKM_OK;
 }
 
-template <typename P, typename C, typename F>
-int run_fused(P const& args, int pass_mode_check, F&& fn) {
-    (void)pass_mode_check;
-    return fn(args);
-}
-
 }  // namespace
 
 extern "C" {
@@ -328,3 +322,18 @@ int ckm_generate_mixture_f32(uint32_t d, uint64_t n, uint32_t blobs, uint64_t se
 }
 
 }  // extern "C"
+
+extern "C" int ckm_generate_mixture_ex_f32(const ckm_mixture_spec* spec, uint64_t n, uint64_t first, float* points,
+                                           uint64_t stride, ckm_stream_t stream) {
+    if (!spec) return fail(CKM_ERR_INVALID_ARGUMENT, "spec is NULL");
+    if (spec->num_features == 0 || spec->num_blobs == 0)
+        return fail(CKM_ERR_INVALID_ARGUMENT, "num_features and num_blobs must be >= 1");
+    if (spec->sigma_dist && !(spec->sigma_lo > 0.0f && spec->sigma_hi > 0.0f))
+        return fail(CKM_ERR_INVALID_ARGUMENT, "log-uniform sigma needs positive bounds");
+    if (n == 0) return CKM_OK;
+    if (!points) return fail(CKM_ERR_INVALID_ARGUMENT, "points NULL");
+    if (stride < n) return fail(CKM_ERR_INVALID_ARGUMENT, "points_stride < num_points");
+    return launch_generate_ex_f32(spec->num_features, n, spec->num_blobs, spec->seed, spec->center_dist,
+                                  spec->center_a, spec->center_b, spec->sigma_dist, spec->sigma_lo, spec->sigma_hi,
+                                  spec->dirichlet, first, points, stride, (cudaStream_t)stream);
+}

@@ -289,6 +289,73 @@ __global__ void __launch_bounds__(256) generate_kernel(uint32_t d, uint64_t n, u
     }
 }
 
+__device__ __forceinline__ float normal01(uint32_t a, uint32_t b, int which) {
+    const float rad = sqrtf(-2.0f * logf(u01(a)));
+    float sn, cs;
+    sincospif(2.0f * u01(b), &sn, &cs);
+    return rad * (which ? sn : cs);
+}
+
+// Mixture with a chosen centre law (uniform in [a, b] or normal with mean a
+// and standard deviation b), sigma law (uniform or log-uniform in [lo, hi])
+// and component weights (equal, or Dirichlet(1): normalised Exp(1) draws).
+// The weights' cumulative table is rebuilt in shared memory by every CTA.
+__global__ void __launch_bounds__(256) generate_ex_kernel(uint32_t d, uint64_t n, uint32_t blobs, uint64_t seed,
+                                                          int center_dist, float ca, float cb, int sigma_dist,
+                                                          float slo, float shi, int dirichlet, uint64_t first,
+                                                          float* out, uint64_t stride) {
+    extern __shared__ float s_cdf[];
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    if (dirichlet) {
+        for (uint32_t b = threadIdx.x; b < blobs; b += blockDim.x) {
+            const U4 r = philox(U4{b, 0u, 0xD1A1u, 4u}, k0, k1);
+            s_cdf[b] = -logf(u01(r.x));
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float acc = 0.f;
+            for (uint32_t b = 0; b < blobs; ++b) {
+                acc += s_cdf[b];
+                s_cdf[b] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    const float total = dirichlet ? s_cdf[blobs - 1] : 1.0f;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t p = first + i;
+        const U4 sel = philox(U4{(uint32_t)p, (uint32_t)(p >> 32), 0xB10Bu, 0u}, k0, k1);
+        uint32_t b;
+        if (dirichlet) {
+            const float u = u01(sel.x) * total;
+            uint32_t lo = 0, hi = blobs - 1;
+            while (lo < hi) {  // first b with cdf[b] >= u
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_cdf[mid] >= u) hi = mid;
+                else lo = mid + 1;
+            }
+            b = lo;
+        } else {
+            b = (uint32_t)(((uint64_t)sel.x * blobs) >> 32);
+        }
+        const U4 sg = philox(U4{b, 0u, 0x516Au, 1u}, k0, k1);
+        const float us = u01(sg.x) - (1.0f / 16777216.0f);
+        const float sigma = sigma_dist ? expf(logf(slo) + (logf(shi) - logf(slo)) * us) : slo + (shi - slo) * us;
+        for (uint32_t f0 = 0; f0 < d; f0 += 4) {
+            const U4 r = philox(U4{(uint32_t)p, (uint32_t)(p >> 32), 0xD47Au + f0, 2u}, k0, k1);
+            const float z[4] = {normal01(r.x, r.y, 0), normal01(r.x, r.y, 1), normal01(r.z, r.w, 0),
+                                normal01(r.z, r.w, 1)};
+            for (uint32_t j = 0; j < 4 && f0 + j < d; ++j) {
+                const uint32_t f = f0 + j;
+                const U4 cc = philox(U4{b, f, 0xCE47u, 3u}, k0, k1);
+                const float centre = center_dist ? ca + cb * normal01(cc.x, cc.y, 0)
+                                                 : ca + (cb - ca) * (u01(cc.x) - (1.0f / 16777216.0f));
+                out[(uint64_t)f * stride + i] = centre + sigma * z[j];
+            }
+        }
+    }
+}
+
 int grid_for(uint64_t work, int block) {
     uint64_t g = (work + block - 1) / block;
     const uint64_t cap = (uint64_t)device_info().sm_count * 8;
@@ -380,6 +447,18 @@ int launch_reduce_parcol_u32(uint64_t cols, uint64_t rows, uint32_t* data, cudaS
 int launch_generate_f32(uint32_t d, uint64_t n, uint32_t blobs, uint64_t seed, float clo, float chi, float slo,
                         float shi, uint64_t first, float* out, uint64_t stride, cudaStream_t s) {
     generate_kernel<<<grid_for(n, 256), 256, 0, s>>>(d, n, blobs, seed, clo, chi, slo, shi, first, out, stride);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "generate launch");
+}
+
+int launch_generate_ex_f32(uint32_t d, uint64_t n, uint32_t blobs, uint64_t seed, int center_dist, float ca,
+                           float cb, int sigma_dist, float slo, float shi, int dirichlet, uint64_t first, float* out,
+                           uint64_t stride, cudaStream_t s) {
+    const size_t smem = dirichlet ? (size_t)blobs * sizeof(float) : 0;
+    if (smem > 48 * 1024) return fail(CKM_ERR_UNSUPPORTED, "Dirichlet weights: at most 12288 blobs");
+    generate_ex_kernel<<<grid_for(n, 256), 256, smem, s>>>(d, n, blobs, seed, center_dist, ca, cb, sigma_dist, slo,
+                                                          shi, dirichlet, first, out, stride);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "generate launch");

@@ -96,5 +96,8 @@ int launch_reduce_parcol_u32(uint64_t cols, uint64_t rows, uint32_t* data, cudaS
 int launch_generate_f32(uint32_t d, uint64_t n, uint32_t blobs, uint64_t seed, float clo, float chi,
                         float slo, float shi, uint64_t first, float* out, uint64_t stride,
                         cudaStream_t s);
+int launch_generate_ex_f32(uint32_t d, uint64_t n, uint32_t blobs, uint64_t seed, int center_dist, float ca,
+                           float cb, int sigma_dist, float slo, float shi, int dirichlet, uint64_t first, float* out,
+                           uint64_t stride, cudaStream_t s);
 
 }  // namespace ckm

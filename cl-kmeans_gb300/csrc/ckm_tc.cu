@@ -8,15 +8,17 @@
 //     elected thread issues d_pad/16 tcgen05.mma (M=128, N=256, K=16, f32
 //     accumulation in tensor memory), commit -> mbarrier;
 //   - each thread owns one point (= one TMEM lane), reads its 256 scores with
-//     tcgen05.ld and keeps the best and second-best score and the best index;
-//   - a rigorous error bound certifies the label: bf16 rounding of both
-//     operands (2^-9 relative each), f32 accumulation, and the FP32 rounding
-//     of the reference distance itself.  If the gap between the two best
-//     scores exceeds twice the bound, no other cluster can win the exact
-//     FP32 comparison of kmeans_naive.cpp:48-63, so the label is the
-//     reference's.  Otherwise the point goes on a list and tc_recheck_kernel
-//     recomputes it with the reference arithmetic over all clusters;
-//   - certified points add their FP32 coordinates into the FP64 scratch.
+//     tcgen05.ld and keeps its TOPK + 1 smallest scores (TOPK clusters);
+//   - a rigorous per-point error bound covers the bf16 rounding of both
+//     operands (2^-9 relative each), the f32 accumulation and the FP32
+//     rounding of the reference distance itself.  A cluster whose score is
+//     more than twice the bound above the best score cannot win the exact
+//     FP32 comparison of kmeans_naive.cpp:48-63.  So: one cluster within the
+//     bound -> that is the reference's label; 2..TOPK clusters within it ->
+//     the thread computes exactly those distances with the reference
+//     arithmetic (ascending cluster order, strict '<'); more -> the point
+//     goes on a list for tc_recheck_kernel (all clusters, exact);
+//   - resolved points add their FP32 coordinates into the FP64 scratch.
 // Empty (NaN) and padding clusters get zero rows and |c|^2 = +inf, so they
 // never win, as NaN never wins in the reference.
 #include <cuda.h>
@@ -37,6 +39,7 @@ namespace {
 constexpr int TC_M = 128;        // points per CTA (TMEM lanes)
 constexpr int TC_N = 256;        // clusters per chunk (TMEM columns)
 constexpr int TC_THREADS = 128;  // one thread per point
+constexpr int TOPK = 8;          // candidates resolved in the kernel by exact arithmetic
 
 // --------------------------------------------------------------------------
 // Preparation kernels
@@ -64,7 +67,8 @@ __global__ void tc_prepare_points_kernel(const float* __restrict__ P, uint64_t n
 // rows zeroed), |c|^2 (+inf for those rows), and max |c| over valid rows.
 __global__ void tc_prepare_centroids_kernel(const float* __restrict__ C, uint32_t k, uint32_t d, uint32_t k_pad,
                                             uint32_t d_pad, __nv_bfloat16* __restrict__ out,
-                                            float* __restrict__ cnorm2, unsigned int* __restrict__ cmax_bits) {
+                                            float* __restrict__ cnorm2, unsigned int* __restrict__ cmax_bits,
+                                            float* __restrict__ rowmajor) {
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < k_pad; c += gridDim.x * blockDim.x) {
         bool valid = c < k;
         double s = 0.0;
@@ -79,6 +83,8 @@ __global__ void tc_prepare_centroids_kernel(const float* __restrict__ C, uint32_
         for (uint32_t f = 0; f < d_pad; ++f)
             row[f] = __float2bfloat16_rn((valid && f < d) ? C[(uint64_t)f * k + c] : 0.0f);
         cnorm2[c] = valid ? (float)s : __int_as_float(0x7f800000);
+        if (c < k)  // FP32 row-major copy: one candidate's features are contiguous
+            for (uint32_t f = 0; f < d; ++f) rowmajor[(uint64_t)c * d + f] = C[(uint64_t)f * k + c];
         if (valid) atomicMax(cmax_bits, __float_as_uint((float)sqrt(s)));  // non-negative floats order as uints
     }
 }
@@ -87,7 +93,8 @@ __global__ void tc_prepare_centroids_kernel(const float* __restrict__ C, uint32_
 // Labeling kernel
 // --------------------------------------------------------------------------
 struct TcParams {
-    const float* points;      // FP32 column-major [d][n] (for the sums)
+    const float* points;      // FP32 column-major [d][n] (sums, exact candidate distances)
+    const float* centroids;   // FP32 row-major [k][d] copy (exact candidate distances)
     const float* norms;       // |x~| per point
     const float* cnorm2;      // [k_pad]
     const unsigned int* cmax_bits;
@@ -144,8 +151,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                               umma::smem_u32(&bar_b));
     }
 
-    float best = __int_as_float(0x7f800000), second = best;
-    uint32_t best_i = 0;
+    // the TOPK + 1 smallest scores (ascending) and the clusters of the first TOPK
+    float top[TOPK + 1];
+    uint32_t top_i[TOPK];
+#pragma unroll
+    for (int t = 0; t <= TOPK; ++t) top[t] = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int t = 0; t < TOPK; ++t) top_i[t] = 0xffffffffu;
     const uint32_t nchunks = prm.k_pad / TC_N;
     bool ok = true;
     for (uint32_t j = 0; j < nchunks; ++j) {
@@ -193,14 +205,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             umma::tmem_ld16(tmem + lane_base + c0, v);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const float s = fmaf(-2.0f, v[i], s_cn[c0 + i]);
-                const uint32_t c = j * TC_N + c0 + i;
-                if (s < best) {
-                    second = best;
-                    best = s;
-                    best_i = c;
-                } else if (s < second) {
-                    second = s;
+                float s = fmaf(-2.0f, v[i], s_cn[c0 + i]);
+                if (s < top[TOPK]) {  // rare after the first clusters: one compare per score
+                    uint32_t c = j * TC_N + c0 + i;
+#pragma unroll
+                    for (int t = 0; t < TOPK; ++t) {
+                        if (s < top[t]) {
+                            const float tv = top[t];
+                            const uint32_t ti = top_i[t];
+                            top[t] = s;
+                            top_i[t] = c;
+                            s = tv;
+                            c = ti;
+                        }
+                    }
+                    top[TOPK] = fminf(top[TOPK], s);
                 }
             }
         }
@@ -214,14 +233,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // certificate (see the file comment for the derivation)
             const float xn = prm.norms[p] * 1.004f;
             const float cm = __uint_as_float(*prm.cmax_bits) * 1.0001f;
-            const float mag = fmaxf(fabsf(best), fabsf(second));
+            const float mag = fmaxf(fabsf(top[0]), fabsf(top[TOPK]));
             const float bound = 0.0081f * xn * cm + 1.6e-5f * (xn + cm) * (xn + cm) + 1.2e-7f * (cm * cm + mag);
-            const bool certified = (second - best) > 2.0f * bound && best_i < prm.k;
-            if (certified) {
-                prm.labels[p] = best_i;
+            // candidates: clusters whose score is within twice the bound of the
+            // best; every other cluster is certified to lose the exact FP32
+            // comparison against the best candidate
+            const float thr = top[0] + 2.0f * bound;
+            uint32_t label = 0xffffffffu;
+            if (top[0] < __int_as_float(0x7f800000) && top[TOPK] > thr && top_i[0] < prm.k) {
+                if (!(top[1] <= thr)) {
+                    label = top_i[0];  // a single candidate
+                } else {
+                    // 2..TOPK candidates: the reference arithmetic on just those,
+                    // visited in ascending cluster order (strict '<' keeps the
+                    // lowest index among equal distances)
+                    uint32_t cand[TOPK];
+                    int nc = 0;
+#pragma unroll
+                    for (int t = 0; t < TOPK; ++t)
+                        if (top[t] <= thr && top_i[t] < prm.k) cand[nc++] = top_i[t];
+                    for (int a = 1; a < nc; ++a)
+                        for (int b = a; b > 0 && cand[b - 1] > cand[b]; --b) {
+                            const uint32_t tmp = cand[b];
+                            cand[b] = cand[b - 1];
+                            cand[b - 1] = tmp;
+                        }
+                    float bv = FLT_MAX;
+                    uint32_t bi = 0xffffffffu;
+                    for (int a = 0; a < nc; ++a) {
+                        const uint32_t c = cand[a];
+                        float acc = 0.0f;
+                        const float* crow = prm.centroids + (uint64_t)c * prm.d;
+                        for (uint32_t f = 0; f < prm.d; ++f) {
+                            const float t = __ldg(prm.points + (uint64_t)f * prm.n + p) - __ldg(crow + f);
+                            acc = fmaf(t, t, acc);
+                        }
+                        if (acc < bv) {
+                            bv = acc;
+                            bi = c;
+                        }
+                    }
+                    label = bi;  // 0xffffffff (nothing below FLT_MAX) -> full recheck
+                }
+            }
+            if (label != 0xffffffffu) {
+                prm.labels[p] = label;
                 for (uint32_t f = 0; f < prm.d; ++f)
-                    atomicAdd(&prm.sums[(uint64_t)f * prm.k + best_i], (double)__ldg(prm.points + (uint64_t)f * prm.n + p));
-                atomicAdd(&prm.msum[best_i], 1ull);
+                    atomicAdd(&prm.sums[(uint64_t)f * prm.k + label], (double)__ldg(prm.points + (uint64_t)f * prm.n + p));
+                atomicAdd(&prm.msum[label], 1ull);
             } else {
                 const unsigned int slot = atomicAdd(prm.nflagged, 1u);
                 prm.flagged[slot] = (uint32_t)p;
@@ -343,6 +402,8 @@ TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k) {
     L.n_pad = (n + TC_M - 1) / TC_M * TC_M;
     auto a = [](size_t v) { return (v + 255) & ~size_t(255); };
     size_t off = 0;
+    L.cent_rm_off = off;
+    off += a((size_t)k * d * 4);
     L.cent_bf16_off = off;
     off += a((size_t)L.k_pad * L.d_pad * 2);
     L.cnorm2_off = off;
@@ -386,6 +447,7 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
     if (!tc_supported(a.d, a.k)) return fail(CKM_ERR_UNSUPPORTED, "tensor-core path: unsupported shape or device");
     char* ws = static_cast<char*>(a.workspace);
     __nv_bfloat16* cent_bf16 = reinterpret_cast<__nv_bfloat16*>(ws + L.cent_bf16_off);
+    float* cent_rm = reinterpret_cast<float*>(ws + L.cent_rm_off);
     float* cnorm2 = reinterpret_cast<float*>(ws + L.cnorm2_off);
     unsigned int* cmax_bits = reinterpret_cast<unsigned int*>(ws + L.cmax_off);
     uint32_t* flagged = reinterpret_cast<uint32_t*>(ws + L.flagged_off);
@@ -395,7 +457,7 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, 256, s);
     if (e != cudaSuccess) return cuda_fail(e, "tc memset");
     tc_prepare_centroids_kernel<<<(L.k_pad + 255) / 256, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d_pad,
-                                                                      cent_bf16, cnorm2, cmax_bits);
+                                                                      cent_bf16, cnorm2, cmax_bits, cent_rm);
     count_launch();
 
     CUtensorMap tm_p, tm_c;
@@ -405,6 +467,7 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
 
     TcParams prm;
     prm.points = a.points;
+    prm.centroids = cent_rm;
     prm.norms = a.norms;
     prm.cnorm2 = cnorm2;
     prm.cmax_bits = cmax_bits;

@@ -12,7 +12,7 @@ namespace ckm {
 struct TcLayout {
     uint32_t d_pad, k_pad;     // features padded to 64, clusters padded to 256
     uint64_t n_pad;            // points padded to 128
-    size_t cent_bf16_off, cnorm2_off, cmax_off, flagged_off, counters_off, total;  // workspace
+    size_t cent_rm_off, cent_bf16_off, cnorm2_off, cmax_off, flagged_off, counters_off, total;  // workspace
     size_t points_bf16_bytes, norms_bytes;                                       // prepared points
 };
 TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k);

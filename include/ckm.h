@@ -272,6 +272,24 @@ int ckm_batch_info(const ckm_batch *batch, uint32_t *grid, uint32_t *tile_points
                    uint32_t *segments);
 int ckm_batch_destroy(ckm_batch *batch);
 
+/* Mixture with chosen laws: centres uniform in [center_a, center_b]
+ * (center_dist 0) or normal with mean center_a and standard deviation
+ * center_b (1); sigmas uniform (sigma_dist 0) or log-uniform (1) in
+ * [sigma_lo, sigma_hi]; component weights equal (dirichlet 0) or
+ * Dirichlet(1) (1, at most 12288 blobs).  Point p depends only on (seed, p). */
+typedef struct ckm_mixture_spec {
+    uint32_t num_features;
+    uint32_t num_blobs;
+    uint64_t seed;
+    int center_dist;
+    float center_a, center_b;
+    int sigma_dist;
+    float sigma_lo, sigma_hi;
+    int dirichlet;
+} ckm_mixture_spec;
+int ckm_generate_mixture_ex_f32(const ckm_mixture_spec *spec, uint64_t num_points, uint64_t first_point,
+                                float *points, uint64_t points_stride, ckm_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Host-level run: AbstractKmeans<PointT,LabelT,MassT>::operator()          */
 /* (abstract_kmeans.hpp:106-130) through a C ABI, with HOST buffers.  The   */

@@ -164,3 +164,25 @@ def test_generator_is_deterministic_and_chunkable(ckm, cuda):
     assert torch.equal(A, C)
     x = a.cpu().numpy()
     assert np.isfinite(x).all() and np.abs(x).max() < 40.0
+
+
+def test_generator_ex_laws(ckm, cuda):
+    """Normal centres, log-uniform sigmas, Dirichlet(1) weights: deterministic,
+    chunkable, finite, and the spread follows the centre law."""
+    import torch
+    n, d, blobs = 200000, 8, 64
+    a = torch.empty(n * d, dtype=torch.float32, device=cuda)
+    b = torch.empty(n * d, dtype=torch.float32, device=cuda)
+    kw = dict(center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0), dirichlet=True)
+    ckm.generate_mixture_ex(a, n, d, blobs, 5, **kw)
+    ckm.generate_mixture_ex(b, n, d, blobs, 5, **kw)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    c = torch.zeros(n * d, dtype=torch.float32, device=cuda)
+    ckm.generate_mixture_ex(c[1000:], n - 1000, d, blobs, 5, first_point=1000, stride=n, **kw)
+    torch.cuda.synchronize()
+    assert torch.equal(a.view(d, n)[:, 1000:], c.view(d, n)[:, 1000:])
+    x = a.cpu().numpy()
+    assert np.isfinite(x).all()
+    assert 1.0 < x.std() < 4.0          # N(0, 4) centres plus sigma <= 1
+    assert abs(x.mean()) < 1.0

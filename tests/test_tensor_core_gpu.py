@@ -57,11 +57,14 @@ def test_tc_ties_and_empty_clusters(ckm, oracle, cuda):
         pytest.skip("tensor-core path not supported on this device")
     P = blobs(n, d, 16, seed=77, spread=3.0)
     C = oracle.first_x_f32(P, n, d, k).reshape(d, k)
-    C[:, 9] = C[:, 5]          # exact duplicate: the lower index must win, via the recheck
+    C[:, 9] = C[:, 5]          # exact duplicate: the lower index wins among the in-kernel candidates
     C[:, 20] = np.nan          # empty cluster from a previous iteration: never chosen
+    dup = list(range(40, 52))  # twelve more copies of cluster 7: more ties than the kernel keeps,
+    C[:, dup] = C[:, [7]]      # so those points go to the full exact recheck
     C = np.ascontiguousarray(C).reshape(-1)
     (Cin, lab, mass, Cout, st), = run_tc(ckm, cuda, P, n, d, k, C, 1)
     ref = oracle.label_f32(P, n, d, k, C)
     assert np.array_equal(lab, ref)
-    assert not np.any(lab == 9) and not np.any(lab == 20)
-    assert st[0] > 0, "duplicate centroids must send their points to the exact recheck"
+    assert not np.any(lab == 9) and not np.any(lab == 20) and not np.any(np.isin(lab, dup))
+    assert np.any(lab == 5) and np.any(lab == 7)
+    assert st[0] > 0, "more tied clusters than candidates must send their points to the exact recheck"
