@@ -323,7 +323,7 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     """Tensor-core labeling with precision recovery: n = 2^24, d = 128,
     k = 1024, a 1024-component mixture (centres ~ N(0, 4 I), sigma
     log-uniform in [0.25, 1], Dirichlet(1) weights), 20 fixed iterations.
-    One step = one Lloyd iteration via ckm_tc_fused_f32 (bf16 distance GEMM
+    One step = one Lloyd iteration via ckm_tc_fused_f32 (fp16 distance GEMM
     on tcgen05, certified labels, exact FP32 recheck of near-ties, FP64
     sums)."""
     n, d, k, iters = 1 << 24, 128, 1024, 20
@@ -344,6 +344,8 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     warm = max(3, min(args.warmup, 5))
     for i in range(warm):
         ckm.tc_fused(P, tcp, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats, stream)
+        if i == 0:
+            tcp.sort(k, stream)  # cluster-ordered tiles from the first labels (once per run)
     C[0].copy_(C0)
     torch.cuda.synchronize()
     sampler = ClockSampler(0)
@@ -389,10 +391,11 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     line = {
         "metric": "pts*iter/s", "value": n / step_s, "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
         "warmup": warm, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16 distances (tcgen05), f32 recheck, f64 sums",
+        "vs_baseline": None, "dtype": "fp16 distances (tcgen05), f32 exact candidates, f64 sums",
         "data": "synthetic (seeded 1024-component mixture generated on the device)",
         "config": {"workload": "lloyd_tc_n%d_d%d_k%d" % (n, d, k), "n": n, "d": d, "k": k,
                    "centres": "N(0, 4I)", "sigma": "log-uniform [0.25, 1]", "weights": "Dirichlet(1)",
+                   "point_order": "sorted by cluster once, after the first iteration (ckm_tc_sort_points)",
                    "l2": "inputs (%.1f GiB) larger than L2, no flush" % (n * d * 6 / 2 ** 30)},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_source": kind, "traffic": None,

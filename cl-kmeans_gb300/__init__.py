@@ -374,6 +374,8 @@ _TC_SIGS = {
     "ckm_tc_supported": ([ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     "ckm_tc_prepare_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                ctypes.c_void_p], ctypes.c_int),
+    "ckm_tc_sort_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),
     "ckm_tc_fused_f32": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32] + [ctypes.c_void_p] * 7 +
                          [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
                           ctypes.c_void_p], ctypes.c_int),
@@ -393,8 +395,9 @@ def _tc_lib():
 
 
 class TensorCorePoints:
-    """A point set prepared for the tensor-core path (bf16 copy + norms) and
-    the per-(n, d, k) workspace; torch device memory."""
+    """A point set prepared for the tensor-core path (scaled fp16 rows, FP32
+    rows, norm bounds, point indices) and the per-(n, d, k) workspace; torch
+    device memory."""
 
     def __init__(self, points, n, d, stream=None):
         import torch
@@ -405,6 +408,17 @@ class TensorCorePoints:
         check(L.ckm_tc_prepare_points(d, n, _p(points), _p(self.buf), nbytes, _stream(stream)),
               "ckm_tc_prepare_points")
         self.ws = {}
+
+    def sort(self, k, stream=None):
+        """ckm_tc_sort_points: reorder the set by the clusters of the last
+        tc_fused call with k clusters (labels keep the caller's order)."""
+        import torch
+        L = _tc_lib()
+        ws = self.workspace(k)
+        out = torch.empty_like(self.buf)
+        check(L.ckm_tc_sort_points(self.d, self.n, k, _p(self.buf), _p(out), out.numel(), _p(ws), ws.numel(),
+                                   _stream(stream)), "ckm_tc_sort_points")
+        self.buf = out
 
     def workspace(self, k):
         import torch

@@ -9,32 +9,59 @@
 
 namespace ckm {
 
+// Header at the start of a prepared point set (device memory, 256 bytes).
+struct TcPointsHeader {
+    unsigned int maxabs_bits;  // max |x_f| over the finite coordinates (float bits)
+    uint32_t reserved[63];
+};
+
+// Per-iteration device values (start of the workspace, 256 bytes).
+struct TcIterDev {
+    unsigned int nflagged;     // points sent to the full exact recheck
+    unsigned int error;        // nonzero: a bounded device wait ran out
+    unsigned int resolved;     // points resolved among 2+ candidates in the label kernel
+    unsigned int cabs_bits;    // max |c_f| over valid centroids (float bits)
+    unsigned int cmax_bits;    // upper bound of max |c| over valid centroids (float bits)
+    float alpha;               // score = cn2 + alpha * (fp16 dot product)
+    float t0, t1, t2, cm;      // certificate threshold T(xn) = t0 + t1 xn + t2 (xn + cm)^2
+    uint32_t reserved[54];
+};
+
 struct TcLayout {
-    uint32_t d_pad, k_pad;     // features padded to 64, clusters padded to 256
-    uint64_t n_pad;            // points padded to 128
-    size_t cent_rm_off, cent_bf16_off, cnorm2_off, cmax_off, flagged_off, counters_off, total;  // workspace
-    size_t points_bf16_bytes, norms_bytes;                                       // prepared points
+    uint32_t d_pad;            // features padded to 64 (one 128-byte swizzle row of fp16)
+    uint32_t d4;               // features padded to 4 (FP32 row-major copies)
+    uint32_t k_pad;            // clusters padded to a whole chunk
+    uint32_t bn;               // clusters per chunk (TMEM columns per accumulator)
+    uint64_t n_pad;            // points padded to a pair of 128-point tiles
+    // prepared points (ckm_tc_points_bytes), all in the set's own point order:
+    // fp16 rows, norm bounds, FP32 rows, and the caller's index of each point
+    size_t pts_half_off, pts_norm_off, pts_rm_off, pts_orig_off, pts_total;
+    // per-iteration workspace (ckm_tc_workspace_bytes)
+    size_t ws_cent_rm_off, ws_cent_half_off, ws_cn2_off, ws_flagged_off, ws_off_off, ws_cursor_off, ws_perm_off,
+        ws_slabels_off, ws_total;
 };
 TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k);
 bool tc_supported(uint32_t d, uint32_t k);
 
 struct TcArgs {
     const float* points;        // FP32 column-major [d][n]
-    const void* points_bf16;    // prepared: bf16 [n_pad][d_pad]
-    const float* norms;         // prepared: [n_pad]
+    const void* tc_points;      // prepared point set (tc_prepare_points)
     const float* centroids;     // FP32 column-major [d][k]
     float* new_centroids;
     uint32_t* labels;
     uint32_t* masses;
     ScratchView scratch;
-    void* workspace;            // tc_layout(n, d, k).total bytes
+    void* workspace;            // tc_layout(n, d, k).ws_total bytes
     unsigned int* stats;        // optional device [2]: rechecked points, error flag
     uint64_t n;
     uint32_t d, k;
     int mode;
 };
 
-int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* points_bf16, float* norms, cudaStream_t s);
+int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, cudaStream_t s);
+// dst = src reordered by the label order of the last iteration run with `workspace`
+int tc_sort_points(uint64_t n, uint32_t d, uint32_t k, const void* src, void* dst, const void* workspace,
+                   cudaStream_t s);
 int tc_iteration(const TcArgs& a, cudaStream_t s);
 
 }  // namespace ckm

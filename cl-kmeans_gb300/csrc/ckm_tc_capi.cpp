@@ -8,12 +8,9 @@ using namespace ckm;
 
 extern "C" {
 
-size_t ckm_tc_points_bytes(uint64_t n, uint32_t d) {
-    const TcLayout L = tc_layout(n, d, 1);
-    return ((L.points_bf16_bytes + 255) & ~size_t(255)) + L.norms_bytes;
-}
+size_t ckm_tc_points_bytes(uint64_t n, uint32_t d) { return tc_layout(n, d, 1).pts_total; }
 
-size_t ckm_tc_workspace_bytes(uint64_t n, uint32_t d, uint32_t k) { return tc_layout(n, d, k).total; }
+size_t ckm_tc_workspace_bytes(uint64_t n, uint32_t d, uint32_t k) { return tc_layout(n, d, k).ws_total; }
 
 int ckm_tc_supported(uint32_t d, uint32_t k) { return tc_supported(d, k) ? 1 : 0; }
 
@@ -23,10 +20,21 @@ int ckm_tc_prepare_points(uint32_t d, uint64_t n, const float* points, void* tc_
     if (!tc_points || (n > 0 && !points)) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL pointer");
     if (bytes < ckm_tc_points_bytes(n, d)) return fail(CKM_ERR_SCRATCH_TOO_SMALL, "tc_points smaller than ckm_tc_points_bytes");
     if (reinterpret_cast<uintptr_t>(tc_points) % 256) return fail(CKM_ERR_INVALID_ARGUMENT, "tc_points must be 256-byte aligned");
-    const TcLayout L = tc_layout(n, d, 1);
-    char* b = static_cast<char*>(tc_points);
-    float* norms = reinterpret_cast<float*>(b + ((L.points_bf16_bytes + 255) & ~size_t(255)));
-    return tc_prepare_points(points, n, d, b, norms, (cudaStream_t)stream);
+    return tc_prepare_points(points, n, d, tc_points, (cudaStream_t)stream);
+}
+
+int ckm_tc_sort_points(uint32_t d, uint64_t n, uint32_t k, const void* tc_points, void* sorted_tc_points,
+                       size_t bytes, const void* workspace, size_t workspace_bytes, ckm_stream_t stream) {
+    if (d == 0 || k == 0) return fail(CKM_ERR_INVALID_ARGUMENT, "num_features and num_clusters must be >= 1");
+    if (!tc_points || !sorted_tc_points || !workspace) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (tc_points == sorted_tc_points) return fail(CKM_ERR_INVALID_ARGUMENT, "the sorted set needs its own buffer");
+    if (bytes < ckm_tc_points_bytes(n, d)) return fail(CKM_ERR_SCRATCH_TOO_SMALL, "sorted_tc_points smaller than ckm_tc_points_bytes");
+    if (workspace_bytes < ckm_tc_workspace_bytes(n, d, k))
+        return fail(CKM_ERR_SCRATCH_TOO_SMALL, "workspace smaller than ckm_tc_workspace_bytes(n, d, k)");
+    if (reinterpret_cast<uintptr_t>(tc_points) % 256 || reinterpret_cast<uintptr_t>(sorted_tc_points) % 256 ||
+        reinterpret_cast<uintptr_t>(workspace) % 256)
+        return fail(CKM_ERR_INVALID_ARGUMENT, "buffers must be 256-byte aligned");
+    return tc_sort_points(n, d, k, tc_points, sorted_tc_points, workspace, (cudaStream_t)stream);
 }
 
 int ckm_tc_fused_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, const void* tc_points,
@@ -48,12 +56,9 @@ int ckm_tc_fused_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, co
     if (n > 0 && (!points || !labels)) return fail(CKM_ERR_INVALID_ARGUMENT, "points/labels NULL");
     if (!old_centroids) return fail(CKM_ERR_INVALID_ARGUMENT, "old_centroids NULL");
     if (mode != CKM_MODE_DEFER && (!new_centroids || !masses)) return fail(CKM_ERR_INVALID_ARGUMENT, "outputs NULL");
-    const TcLayout L = tc_layout(n, d, k);
-    const char* b = static_cast<const char*>(tc_points);
     TcArgs a;
     a.points = points;
-    a.points_bf16 = b;
-    a.norms = reinterpret_cast<const float*>(b + ((L.points_bf16_bytes + 255) & ~size_t(255)));
+    a.tc_points = tc_points;
     a.centroids = old_centroids;
     a.new_centroids = new_centroids;
     a.labels = labels;

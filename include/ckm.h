@@ -122,15 +122,16 @@ int ckm_fused_f32_noalloc(uint32_t num_features, uint64_t num_points, uint32_t n
                           uint32_t *labels, uint32_t *masses, int mode, ckm_stream_t stream);
 
 /* Tensor-core fused iteration for large k*d (d <= 256): the same contract as
- * ckm_fused_f32, computed as a bf16 distance GEMM on the tensor cores
- * (tcgen05, f32 accumulation), whose labels are certified against an error
- * bound; points whose two best scores are too close for the bound are
- * recomputed with the reference's exact FP32 arithmetic, so the labels are
- * the reference's.  Sums merge in FP64.  Replaces the same functor as
+ * ckm_fused_f32, computed as an fp16 distance GEMM on the tensor cores
+ * (tcgen05, f32 accumulation; operands scaled by powers of two), whose labels
+ * are certified against a rigorous error bound; the clusters the bound cannot
+ * separate are recomputed with the reference's exact FP32 arithmetic, so the
+ * labels are the reference's.  Sums merge in FP64.  Replaces the same functor as
  * ckm_fused_f32 (fused_factory.hpp:34-53) for shapes where the distance
  * block is a dense contraction.
  *   tc_points: ckm_tc_points_bytes(n, d) bytes, filled once per point set by
- *              ckm_tc_prepare_points (a bf16 copy + norms);
+ *              ckm_tc_prepare_points (scaled fp16 rows, FP32 rows, norm
+ *              bounds, point indices), or by ckm_tc_sort_points;
  *   workspace: ckm_tc_workspace_bytes(n, d, k) bytes;
  *   stats:     optional device uint32[2]: points rechecked exactly, and a
  *              nonzero error flag if a bounded device wait ran out. */
@@ -139,6 +140,16 @@ size_t ckm_tc_workspace_bytes(uint64_t num_points, uint32_t num_features, uint32
 int ckm_tc_supported(uint32_t num_features, uint32_t num_clusters);
 int ckm_tc_prepare_points(uint32_t num_features, uint64_t num_points, const float *points, void *tc_points,
                           size_t tc_points_bytes, ckm_stream_t stream);
+/* Writes into sorted_tc_points (its own ckm_tc_points_bytes(n, d) buffer) the
+ * prepared set tc_points reordered by the clusters of the last
+ * ckm_tc_fused_f32 call made with `workspace` for the same set and k.  Points
+ * of one cluster then share the label kernel's 128-point tiles, which keeps
+ * its candidate tests coherent across a warp.  Labels, masses and centroids
+ * stay in the caller's point order: the set carries each point's index.  No
+ * counterpart in the reference. */
+int ckm_tc_sort_points(uint32_t num_features, uint64_t num_points, uint32_t num_clusters, const void *tc_points,
+                       void *sorted_tc_points, size_t tc_points_bytes, const void *workspace,
+                       size_t workspace_bytes, ckm_stream_t stream);
 int ckm_tc_fused_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters, const float *points,
                      const void *tc_points, const float *old_centroids, float *new_centroids, uint32_t *labels,
                      uint32_t *masses, void *scratch, size_t scratch_bytes, void *workspace,

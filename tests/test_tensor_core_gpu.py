@@ -68,3 +68,107 @@ def test_tc_ties_and_empty_clusters(ckm, oracle, cuda):
     assert not np.any(lab == 9) and not np.any(lab == 20) and not np.any(np.isin(lab, dup))
     assert np.any(lab == 5) and np.any(lab == 7)
     assert st[0] > 0, "more tied clusters than candidates must send their points to the exact recheck"
+
+
+@pytest.mark.parametrize("scale,offset", [(1e6, 0.0), (1e-6, 0.0), (1.0, -3e3), (3e-30, 1e-29)])
+def test_tc_extreme_magnitudes(ckm, oracle, cuda, scale, offset):
+    """Power-of-two operand scaling keeps fp16 in range for any magnitude;
+    labels stay the reference's."""
+    n, d, k = 8192, 48, 96
+    if not ckm.tc_supported(d, k):
+        pytest.skip("tensor-core path not supported on this device")
+    P = (blobs(n, d, 24, seed=5, spread=4.0, sigma=0.6).astype(np.float64) * scale + offset).astype(np.float32)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    for Cin, lab, mass, Cout, st in run_tc(ckm, cuda, P, n, d, k, C0, 2):
+        assert st[1] == 0
+        check_iter(oracle, P, n, d, k, Cin, lab, mass, Cout)
+
+
+@pytest.mark.parametrize("d", [1, 3, 7, 200])
+def test_tc_small_and_odd_feature_counts(ckm, oracle, cuda, d):
+    n, k = 6001, 150
+    if not ckm.tc_supported(d, k):
+        pytest.skip("tensor-core path not supported on this device")
+    P = blobs(n, d, 40, seed=d, spread=5.0, sigma=0.7)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    for Cin, lab, mass, Cout, st in run_tc(ckm, cuda, P, n, d, k, C0, 2):
+        assert st[1] == 0
+        check_iter(oracle, P, n, d, k, Cin, lab, mass, Cout)
+
+
+def test_tc_nan_points_get_label_zero(ckm, oracle, cuda):
+    """A point with a NaN coordinate has NaN distances: the reference keeps
+    label 0 (nothing is below FLT_MAX)."""
+    n, d, k = 3000, 32, 64
+    if not ckm.tc_supported(d, k):
+        pytest.skip("tensor-core path not supported on this device")
+    P = blobs(n, d, 16, seed=11).reshape(d, n)
+    P[3, [17, 1000, 2999]] = np.nan
+    P = np.ascontiguousarray(P).reshape(-1)
+    C = oracle.first_x_f32(P, n, d, k)
+    (Cin, lab, mass, Cout, st), = run_tc(ckm, cuda, P, n, d, k, C, 1)
+    ref = oracle.label_f32(P, n, d, k, C)
+    assert np.array_equal(lab, ref)
+    assert lab[17] == 0 and lab[1000] == 0 and lab[2999] == 0
+    assert np.array_equal(mass, oracle.mass_u32(ref, k))
+
+
+def test_tc_defer_then_finalize_over_chunks(ckm, oracle, cuda):
+    """CKM_MODE_DEFER over two point chunks, then ckm_finalize_f32: the same
+    centroids and masses as one call over all points (the buffered pipeline's
+    use of the fused functor)."""
+    import torch
+    n, d, k = 12000, 64, 200
+    if not ckm.tc_supported(d, k):
+        pytest.skip("tensor-core path not supported on this device")
+    P = blobs(n, d, 50, seed=21, spread=4.0, sigma=0.5)
+    C = oracle.first_x_f32(P, n, d, k)
+    ref = oracle.label_f32(P, n, d, k, C)
+    Pm = P.reshape(d, n)
+    h = 7001
+    dC = to_dev(C, cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    labs = []
+    for lo, hi in ((0, h), (h, n)):
+        part = np.ascontiguousarray(Pm[:, lo:hi]).reshape(-1)
+        m = hi - lo
+        dP = to_dev(part, cuda)
+        tcp = ckm.TensorCorePoints(dP, m, d)
+        dL = torch.zeros(m, dtype=torch.int32, device=cuda)
+        ckm.tc_fused(dP, tcp, dC, dC, dL, None, S, m, d, k, ckm.MODE_DEFER)
+        torch.cuda.synchronize()
+        labs.append(dL.cpu().numpy().view(np.uint32).copy())
+    lab = np.concatenate(labs)
+    assert np.array_equal(lab, ref)
+    out = torch.zeros(k * d, dtype=torch.float32, device=cuda)
+    dM = torch.zeros(k, dtype=torch.int32, device=cuda)
+    ckm.finalize(out, dM, S, d, k)
+    torch.cuda.synchronize()
+    assert np.array_equal(dM.cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+    check_centroids(oracle, P, n, d, k, ref, out.cpu().numpy())
+
+
+def test_tc_sorted_point_set_keeps_caller_order(ckm, oracle, cuda):
+    """ckm_tc_sort_points reorders the prepared set by the last labels; the
+    following iterations still return labels in the caller's point order,
+    equal to the oracle's, and the same centroids as the unsorted set."""
+    import torch
+    n, d, k = 30011, 96, 300
+    if not ckm.tc_supported(d, k):
+        pytest.skip("tensor-core path not supported on this device")
+    P = blobs(n, d, 60, seed=31, spread=4.0, sigma=0.6)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    dP = to_dev(P, cuda)
+    tcp = ckm.TensorCorePoints(dP, n, d)
+    bufs = [to_dev(C0, cuda), torch.zeros(k * d, dtype=torch.float32, device=cuda)]
+    dL = torch.zeros(n, dtype=torch.int32, device=cuda)
+    dM = torch.zeros(k, dtype=torch.int32, device=cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    for it in range(4):
+        Cin = bufs[it % 2].cpu().numpy()
+        ckm.tc_fused(dP, tcp, bufs[it % 2], bufs[(it + 1) % 2], dL, dM, S, n, d, k, ckm.MODE_FINALIZE)
+        torch.cuda.synchronize()
+        check_iter(oracle, P, n, d, k, Cin, dL.cpu().numpy().view(np.uint32), dM.cpu().numpy().view(np.uint32),
+                   bufs[(it + 1) % 2].cpu().numpy())
+        if it < 2:
+            tcp.sort(k)   # sorted by the labels of this iteration (twice: a sorted set sorts again)
