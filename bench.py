@@ -352,15 +352,19 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     sampler.start()
     time.sleep(0.3)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    rechecked = []
+    rechecked, resolved, overflowed = [], [], []
+    counters = torch.zeros(4, dtype=torch.int32, device=dev)
     launches0 = ckm.launch_count()
     for i in range(steps):
         evs[i][0].record(stream)
         ckm.tc_fused(P, tcp, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats, stream)
         evs[i][1].record(stream)
         torch.cuda.synchronize()
-        st = stats.cpu().numpy()
+        tcp.counters(k, counters, stream)
+        st = counters.cpu().numpy()
         rechecked.append(int(st[0]))
+        resolved.append(int(st[2]))
+        overflowed.append(int(st[3]))
         if st[1]:
             raise RuntimeError("tensor-core kernel reported a timed-out device wait")
     gpu_launches = ckm.launch_count() - launches0
@@ -401,6 +405,8 @@ def run_tensor_core_workload(args, ckm, torch, dev):
                      "frac": achieved / peak, "peak_source": kind, "traffic": None,
                      "algorithmic_flops_per_step": flops},
         "rechecked_points_per_step": rechecked,
+        "resolved_in_kernel_per_step": resolved,
+        "overflowed_per_step": overflowed,
         "simt_fp32_step_ms": simt_s * 1e3 if simt_s is not None else None,
         "cpu_baseline": cpu, "gpu_launches": int(gpu_launches), "clocks": clocks,
     }

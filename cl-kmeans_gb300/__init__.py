@@ -374,6 +374,7 @@ _TC_SIGS = {
     "ckm_tc_supported": ([ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     "ckm_tc_prepare_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                ctypes.c_void_p], ctypes.c_int),
+    "ckm_tc_counters": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ckm_tc_sort_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
                             ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),
     "ckm_tc_fused_f32": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32] + [ctypes.c_void_p] * 7 +
@@ -419,6 +420,11 @@ class TensorCorePoints:
         check(L.ckm_tc_sort_points(self.d, self.n, k, _p(self.buf), _p(out), out.numel(), _p(ws), ws.numel(),
                                    _stream(stream)), "ckm_tc_sort_points")
         self.buf = out
+
+    def counters(self, k, out, stream=None):
+        """ckm_tc_counters into the int32 device tensor out[4]: rechecked,
+        error, resolved among 2+ candidates, overflowed."""
+        check(_tc_lib().ckm_tc_counters(_p(self.workspace(k)), _p(out), _stream(stream)), "ckm_tc_counters")
 
     def workspace(self, k):
         import torch

@@ -9,11 +9,12 @@
 //
 //   - points and centroids are scaled by powers of two (sx, sc) so that every
 //     coordinate fits fp16 (|.| <= 2^15) and rounded to fp16 once;
-//   - a rigorous bound T(x) covers the fp16 rounding of both operands (2^-11
-//     relative, 2^-25 absolute below the normal range), the f32 accumulation
-//     (one ulp per addition), the rounding of |c|^2 and of the score itself,
-//     the FP32 rounding of the reference distance ((d + 2) 2^-24 relative)
-//     and FP32 underflow (2^-150 absolute per operation).  A cluster whose score is more than T above the best score
+//   - a rigorous bound T(x) covers the fp16 rounding of both operands (by the
+//     norms of the actual rounding errors, measured when the operands are
+//     made, through Cauchy-Schwarz), the f32 accumulation (one ulp per
+//     addition), the rounding of |c|^2 and of the score itself, the FP32
+//     rounding of the reference distance ((d + 2) 2^-24 relative) and FP32
+//     underflow (2^-150 absolute per operation).  A cluster whose score is more than T above the best score
 //     cannot reach or tie the reference's minimum, so the reference's label
 //     is among the clusters within T of the best (the candidates);
 //   - one candidate: that is the label.  2..CAP candidates: the kernel
@@ -56,7 +57,6 @@ constexpr int MMA_WARP = 9;
 constexpr int LABEL_THREADS = 320;
 constexpr int CAP = 8;               // candidates kept per point in the label kernel
 constexpr int GRP = 16;              // scores per warp-uniform append test
-static_assert(CAP <= 8, "queue entries pack a list slot into 3 bits");
 constexpr int MAX_A_STAGES = 2;
 constexpr int MAX_B_STAGES = 4;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // bounded waits give up after 2 s
@@ -179,7 +179,8 @@ __global__ void __launch_bounds__(256) tc_points_convert_kernel(const float* __r
                                                                 uint32_t d_pad, uint32_t d4,
                                                                 const TcPointsHeader* __restrict__ hdr,
                                                                 __half* __restrict__ ph, float* __restrict__ norms,
-                                                                float* __restrict__ prm, uint32_t* __restrict__ orig) {
+                                                                float* __restrict__ errn, float* __restrict__ prm,
+                                                                uint32_t* __restrict__ orig) {
     extern __shared__ float s_tile[];  // [d][33]
     const float sx = ldexpf(1.0f, scale_exponent(__uint_as_float(hdr->maxabs_bits)));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -190,18 +191,27 @@ __global__ void __launch_bounds__(256) tc_points_convert_kernel(const float* __r
         for (int r = warp; r < 32; r += 8) {
             const uint64_t q = p0 + r;
             if (q >= n) break;
-            float ss = 0.0f;
+            float ss = 0.0f, ee = 0.0f;
             for (uint32_t f = lane; f < d_pad; f += 32) {
                 const float v = f < d ? s_tile[f * 33 + r] : 0.0f;
                 ss = fmaf(v, v, ss);
-                ph[q * d_pad + f] = __float2half_rn(v * sx);
+                const __half h = __float2half_rn(v * sx);
+                ph[q * d_pad + f] = h;
+                const float e = __half2float(h) - v * sx;  // exact: both within a factor 2 (or e = -v sx)
+                ee = fmaf(e, e, ee);
             }
             for (uint32_t f = lane; f < d4; f += 32) prm[q * d4 + f] = f < d ? s_tile[f * 33 + r] : 0.0f;
-            for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                ee += __shfl_xor_sync(0xffffffffu, ee, o);
+            }
             // FP32 sum of d + 5 non-negative terms: relative error below
             // (d + 5) 2^-24 < 2^-14; the square root adds half an ulp
             if (lane == 0) {
                 norms[q] = sqrtf(ss * (1.0f + 0x1p-14f)) * (1.0f + 0x1p-20f);
+                // + d 2^-149: v sx may have been rounded where it fell below
+                // FP32's normal range
+                errn[q] = (sqrtf(ee * (1.0f + 0x1p-14f)) * (1.0f + 0x1p-20f) + (float)d * 0x1p-149f) / sx;
                 orig[q] = (uint32_t)q;
             }
         }
@@ -247,39 +257,50 @@ __global__ void tc_centroid_stats_kernel(const float* __restrict__ C, uint32_t k
 }
 
 // fp16 centroids scaled by sc, K-major [k_pad][d_pad] (invalid and padding
-// rows zero), and the per-iteration scale and certificate constants.
+// rows zero), and a bound of the fp16 rounding error of the valid rows.
 __global__ void tc_centroid_pack_kernel(const float* __restrict__ C, uint32_t k, uint32_t d, uint32_t k_pad,
-                                        uint32_t d_pad, const float* __restrict__ cn2,
-                                        const TcPointsHeader* __restrict__ hdr, __half* __restrict__ ch,
+                                        uint32_t d_pad, const float* __restrict__ cn2, __half* __restrict__ ch,
                                         TcIterDev* it) {
     const int ec = scale_exponent(__uint_as_float(it->cabs_bits));
     const float sc = ldexpf(1.0f, ec);
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < k_pad; c += gridDim.x * blockDim.x) {
         const bool valid = c < k && cn2[c] < __int_as_float(0x7f800000);
         __half* row = ch + (uint64_t)c * d_pad;
-        for (uint32_t f = 0; f < d_pad; ++f)
-            row[f] = __float2half_rn((valid && f < d) ? C[(uint64_t)f * k + c] * sc : 0.0f);
+        double ee = 0.0;
+        for (uint32_t f = 0; f < d_pad; ++f) {
+            const float b = (valid && f < d) ? C[(uint64_t)f * k + c] * sc : 0.0f;
+            const __half h = __float2half_rn(b);
+            row[f] = h;
+            const double e = (double)__half2float(h) - (double)b;
+            ee = fma(e, e, ee);
+        }
+        if (valid)
+            atomicMax(&it->fmax_bits,
+                      __float_as_uint(__double2float_ru((sqrt(ee) * (1.0 + 0x1p-40) + d * 0x1p-149) / sc)));
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const int ex = scale_exponent(__uint_as_float(hdr->maxabs_bits));
-        const double sx = ldexp(1.0, ex), scd = ldexp(1.0, ec);
-        const double cm = (double)__uint_as_float(it->cmax_bits);
-        const double u = 0x1p-11, eta = 0x1p-25, gam = 2.0 * d_pad * 0x1p-23, rd = sqrt((double)d);
-        const double safety = 1.0 + 0x1p-10;
-        const double a1 = 4.0 * (2.0 * u + u * u + gam * (1.0 + u) * (1.0 + u));
-        const double a3 = 4.0 * eta * (1.0 + u) * rd;
-        const double t1 = (a1 * cm + a3 / scd) * safety;
-        // the last term: results that underflow to subnormals or zero (|c|^2,
-        // the score, the reference's t and fma chain) carry absolute errors up
-        // to 2^-150 each, which no relative bound covers
-        const double t0 = (a3 * cm / sx + 4.0 * d * eta * eta / (sx * scd)) * safety + (d + 8.0) * 0x1p-146;
-        const double t2 = (2.0 * 0x1p-23 * 1.01 + 2.0 * (d + 2.0) * 0x1p-24 * 1.01) * safety;
-        it->alpha = (float)(-2.0 / (sx * scd));  // a power of two: exact
-        it->t0 = __double2float_ru(t0);
-        it->t1 = __double2float_ru(t1);
-        it->t2 = __double2float_ru(t2);
-        it->cm = (float)cm;
-    }
+}
+
+// The per-iteration scale and certificate constants (one thread).  With x
+// the point, e its fp16 rounding error (both unscaled), cm >= max |c| and
+// fm >= max |fp16 error of c| over valid centroids, g = 2 d_pad 2^-23 (f32
+// accumulation, one ulp per addition) and rho = (d + 2) 2^-24 (the
+// reference's FP32 distance):
+//   |score error| <= 2 (|x| fm + |e| (cm + fm) + g (|x| + |e|)(cm + fm))
+//                    + 2^-23 (|x| + cm)^2       (|c|^2 and the score rounded)
+//   T = 2 |score error| + 2 rho (|x| + cm)^2 + (d + 8) 2^-146 (underflow)
+// (Cauchy-Schwarz on the exact rounding errors: |sum e_f c_f| <= |e||c|.)
+__global__ void tc_params_kernel(uint32_t d, uint32_t d_pad, const TcPointsHeader* __restrict__ hdr, TcIterDev* it) {
+    const int ex = scale_exponent(__uint_as_float(hdr->maxabs_bits));
+    const int ec = scale_exponent(__uint_as_float(it->cabs_bits));
+    const double sx = ldexp(1.0, ex), scd = ldexp(1.0, ec);
+    const double cm = (double)__uint_as_float(it->cmax_bits), fm = (double)__uint_as_float(it->fmax_bits);
+    const double gam = 2.0 * d_pad * 0x1p-23, safety = 1.0 + 0x1p-10;
+    it->alpha = (float)(-2.0 / (sx * scd));  // a power of two: exact
+    it->t1 = __double2float_ru((4.0 * fm + 4.0 * gam * (cm + fm)) * safety);
+    it->te = __double2float_ru((4.0 * (cm + fm) + 4.0 * gam * (cm + fm)) * safety);
+    it->t2 = __double2float_ru((2.0 * 0x1p-23 * 1.01 + 2.0 * (d + 2.0) * 0x1p-24 * 1.01) * safety);
+    it->t0 = __double2float_ru((d + 8.0) * 0x1p-146);
+    it->cm = __double2float_ru(cm);
 }
 
 // --------------------------------------------------------------------------
@@ -287,6 +308,7 @@ __global__ void tc_centroid_pack_kernel(const float* __restrict__ C, uint32_t k,
 // --------------------------------------------------------------------------
 struct LabelParams {
     const float* norms;          // upper bound of |x| per point
+    const float* errn;           // upper bound of |fp16(x sx) / sx - x| per point
     const float* x_rm;           // FP32 points, row-major [n][d4]
     const uint32_t* orig;        // caller's index of each point of the set
     const float* c_rm;           // FP32 centroids, row-major [k][d4]
@@ -296,6 +318,8 @@ struct LabelParams {
     uint32_t* slabels;           // the set's order
     uint32_t* counts;            // points per label in this call
     uint32_t* flagged;           // points for the full recheck
+    uint32_t* res_pts;           // points with 2+ candidates (tc_resolve_kernel)
+    uint32_t* res_cands;         // their candidates, CAP per point, NONE-padded
     uint64_t n;
     uint32_t d, d4, d_pad, k, chunks, num_pairs, a_stages, b_stages;
 };
@@ -326,7 +350,6 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
     const uint32_t a_bytes = PAIR_M * prm.d_pad * 2u, b_bytes = BN * prm.d_pad * 2u;
     const uint32_t sA = base, sB = base + prm.a_stages * a_bytes;
     float2* lists = reinterpret_cast<float2*>(smem_raw + (base - raw) + prm.a_stages * a_bytes + prm.b_stages * b_bytes);
-    uint8_t* queue = reinterpret_cast<uint8_t*>(lists + (CAP + 1) * EPI_THREADS);  // [EPI_WARPS][32 * CAP]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t kblocks = prm.d_pad / 64u;
 
@@ -426,7 +449,8 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
         const uint32_t u = (uint32_t)warp >> 2, lg = (uint32_t)warp & 3u;
         const uint32_t row = lg * 32u + (uint32_t)lane;
         const uint32_t etid = threadIdx.x;
-        const float alpha = prm.it->alpha, t0 = prm.it->t0, t1 = prm.it->t1, t2 = prm.it->t2, cm = prm.it->cm;
+        const float alpha = prm.it->alpha, t0 = prm.it->t0, t1 = prm.it->t1, te = prm.it->te, t2 = prm.it->t2,
+                    cm = prm.it->cm;
         const float2 al2 = make_float2(alpha, alpha);
         const float INF = __int_as_float(0x7f800000);
         const uint32_t lane_addr = tmem + ((lg * 32u) << 16);
@@ -436,7 +460,8 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
             const uint64_t p = (uint64_t)q * PAIR_M + u * TILE_M + row;
             const bool valid = p < prm.n;
             const float xn = valid ? __ldg(prm.norms + p) : 0.0f;
-            const float T = fmaf(t2 * (xn + cm), xn + cm, fmaf(t1, xn, t0)) * (1.0f + 0x1p-10f);
+            const float xe = valid ? __ldg(prm.errn + p) : 0.0f;
+            const float T = fmaf(t2 * (xn + cm), xn + cm, fmaf(te, xe, fmaf(t1, xn, t0))) * (1.0f + 0x1p-10f);
             float m = INF;
             uint32_t cnt = 0;
             bool ovf = false;
@@ -521,12 +546,9 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
             if (aborted) break;
 
             // ---- resolution ----
-            // Filter the list with the final m: entries out of range are marked
-            // NONE.  One candidate: the label.  Two or more: the warp computes
-            // the exact distances of all its lanes' (point, candidate) pairs
-            // 32 at a time, then each such lane takes the smallest distance
-            // below FLT_MAX, the lowest index on a tie (= strict '<' in
-            // ascending cluster order, kmeans_naive.cpp:58-61).
+            // Filter the list with the final m.  One candidate: the label.  Two
+            // or more: a record (point, candidates) for tc_resolve_kernel.
+            // Overflow or no finite score: the full exact recheck.
             const float cut = m + T;
             bool flag = valid && (ovf || !(m > -INF && m < INF));
             uint32_t label = NONE, nc = 0;
@@ -535,57 +557,25 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                     const float2 v = lists[e * EPI_THREADS + etid];
                     const uint32_t c = __float_as_uint(v.y);
                     if (v.x <= cut && c < prm.k) {
+                        lists[nc * EPI_THREADS + etid].y = v.y;  // compact the candidates to the front
                         ++nc;
                         label = c;
-                    } else {
-                        lists[e * EPI_THREADS + etid].y = __uint_as_float(NONE);
                     }
                 }
                 if (nc == 0) flag = true;
             }
             const bool need = valid && !flag && nc >= 2;
-            uint32_t mine = need ? nc : 0u, offs = mine;  // inclusive scan over lanes
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, offs, o);
-                if (lane >= o) offs += y;
-            }
-            const uint32_t total = __shfl_sync(0xffffffffu, offs, 31);
-            if (total) {
-                uint8_t* wq = queue + warp * (32 * CAP);
-                uint32_t w = offs - mine;
-                if (need)
-                    for (uint32_t e = 0; e < cnt; ++e)
-                        if (__float_as_uint(lists[e * EPI_THREADS + etid].y) != NONE) wq[w++] = (uint8_t)((lane << 3) | e);
-                __syncwarp();
-                for (uint32_t b = 0; b < total; b += 32) {
-                    if (b + lane < total) {
-                        const uint32_t ent = wq[b + lane], L = ent >> 3, e = ent & 7u;
-                        const uint32_t et = (uint32_t)warp * 32u + L;
-                        const uint32_t c = __float_as_uint(lists[e * EPI_THREADS + et].y);
-                        const uint64_t pl = (uint64_t)q * PAIR_M + u * TILE_M + lg * 32u + L;
-                        lists[e * EPI_THREADS + et].x =
-                            exact_distance(prm.x_rm + pl * prm.d4, prm.c_rm + (uint64_t)c * prm.d4, prm.d);
-                    }
-                }
-                __syncwarp();
-                if (need) {
-                    float best = FLT_MAX;
-                    uint32_t bi = NONE;
-                    for (uint32_t e = 0; e < cnt; ++e) {
-                        const float2 v = lists[e * EPI_THREADS + etid];
-                        const uint32_t c = __float_as_uint(v.y);
-                        if (c == NONE) continue;
-                        if (v.x < best || (v.x == best && bi != NONE && c < bi)) {
-                            best = v.x;
-                            bi = c;
-                        }
-                    }
-                    label = bi;
-                    if (label == NONE) flag = true;
-                }
-            }
-            if (valid) {
+            const unsigned int needm = __ballot_sync(0xffffffffu, need);
+            uint32_t slot0 = 0;
+            if (lane == 0 && needm) slot0 = atomicAdd(&prm.it->resolved, (unsigned)__popc(needm));
+            slot0 = __shfl_sync(0xffffffffu, slot0, 0);
+            if (need) {
+                const uint32_t slot = slot0 + __popc(needm & ((1u << lane) - 1u));
+                prm.res_pts[slot] = (uint32_t)p;
+                uint32_t* rc = prm.res_cands + (uint64_t)slot * CAP;
+                for (uint32_t e = 0; e < CAP; ++e)
+                    rc[e] = e < nc ? __float_as_uint(lists[e * EPI_THREADS + etid].y) : NONE;
+            } else if (valid) {
                 if (flag) {
                     const unsigned int slot = atomicAdd(&prm.it->nflagged, 1u);
                     prm.flagged[slot] = (uint32_t)p;
@@ -595,9 +585,8 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                     atomicAdd(&prm.counts[label], 1u);
                 }
             }
-            const unsigned int nres = __popc(__ballot_sync(0xffffffffu, need));
-            if (lane == 0 && nres) atomicAdd(&prm.it->resolved, nres);
-            __syncwarp();  // the queue and the lists are reused by the next pair
+            const unsigned int novf = __popc(__ballot_sync(0xffffffffu, valid && ovf));
+            if (lane == 0 && novf) atomicAdd(&prm.it->overflowed, novf);
         }
     }
 
@@ -609,6 +598,79 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
         umma::tmem_dealloc(tmem, 4 * BN);
     }
     if (threadIdx.x == 0 && s_abort) atomicExch(&prm.it->error, 1u);
+}
+
+// --------------------------------------------------------------------------
+// Exact resolution of points with 2..CAP candidates: the reference distance
+// (t = x_f - c_f, acc = fma(t, t, acc), f ascending) of every candidate, in
+// one pass over the point's row; the smallest distance below FLT_MAX wins,
+// the lowest index on a tie (= strict '<' in ascending cluster order,
+// kmeans_naive.cpp:58-61).  Nothing below FLT_MAX: the full recheck.
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) tc_resolve_kernel(const float* __restrict__ x_rm, const float* __restrict__ c_rm,
+                                                         uint32_t d, uint32_t d4, const uint32_t* __restrict__ res_pts,
+                                                         const uint32_t* __restrict__ res_cands,
+                                                         const uint32_t* __restrict__ orig, TcIterDev* it,
+                                                         uint32_t* __restrict__ flagged, uint32_t* __restrict__ labels,
+                                                         uint32_t* __restrict__ slabels, uint32_t* __restrict__ counts) {
+    const unsigned int count = it->resolved;
+    for (unsigned int r = blockIdx.x * blockDim.x + threadIdx.x; r < count; r += gridDim.x * blockDim.x) {
+        const uint32_t p = __ldg(res_pts + r);
+        uint32_t cand[CAP];
+        int nc = 0;
+#pragma unroll
+        for (int j = 0; j < CAP; ++j) {
+            cand[j] = __ldg(res_cands + (uint64_t)r * CAP + j);
+            nc += cand[j] != NONE;
+        }
+        float acc[CAP];
+#pragma unroll
+        for (int j = 0; j < CAP; ++j) acc[j] = 0.0f;
+        const float4* xr = reinterpret_cast<const float4*>(x_rm + (uint64_t)p * d4);
+        uint32_t f = 0;
+        for (; f + 4 <= d; f += 4) {
+            const float4 x = __ldg(xr + f / 4);
+#pragma unroll
+            for (int j = 0; j < CAP; ++j) {
+                if (j < nc) {
+                    const float4 c = __ldg(reinterpret_cast<const float4*>(c_rm + (uint64_t)cand[j] * d4) + f / 4);
+                    float t = x.x - c.x;
+                    acc[j] = fmaf(t, t, acc[j]);
+                    t = x.y - c.y;
+                    acc[j] = fmaf(t, t, acc[j]);
+                    t = x.z - c.z;
+                    acc[j] = fmaf(t, t, acc[j]);
+                    t = x.w - c.w;
+                    acc[j] = fmaf(t, t, acc[j]);
+                }
+            }
+        }
+        for (; f < d; ++f) {
+            const float x = __ldg(x_rm + (uint64_t)p * d4 + f);
+#pragma unroll
+            for (int j = 0; j < CAP; ++j)
+                if (j < nc) {
+                    const float t = x - __ldg(c_rm + (uint64_t)cand[j] * d4 + f);
+                    acc[j] = fmaf(t, t, acc[j]);
+                }
+        }
+        float best = FLT_MAX;
+        uint32_t bi = NONE;
+#pragma unroll
+        for (int j = 0; j < CAP; ++j)
+            if (j < nc && (acc[j] < best || (acc[j] == best && bi != NONE && cand[j] < bi))) {
+                best = acc[j];
+                bi = cand[j];
+            }
+        if (bi == NONE) {
+            const unsigned int slot = atomicAdd(&it->nflagged, 1u);
+            flagged[slot] = p;
+        } else {
+            labels[__ldg(orig + p)] = bi;
+            slabels[p] = bi;
+            atomicAdd(&counts[bi], 1u);
+        }
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -932,6 +994,7 @@ __global__ void __launch_bounds__(256) tc_sort_points_kernel(uint64_t n, uint32_
                                                              const uint32_t* __restrict__ off,
                                                              const uint4* __restrict__ sh, uint4* __restrict__ dh,
                                                              const float* __restrict__ sn, float* __restrict__ dn,
+                                                             const float* __restrict__ se, float* __restrict__ de,
                                                              const float4* __restrict__ sr, float4* __restrict__ dr,
                                                              const uint32_t* __restrict__ so, uint32_t* __restrict__ dor) {
     const bool ordered = __ldg(off + k) == n;
@@ -946,6 +1009,7 @@ __global__ void __launch_bounds__(256) tc_sort_points_kernel(uint64_t n, uint32_
         for (uint32_t c = lane; c < rrow; c += 32) dr[i * rrow + c] = __ldg(sr + src * rrow + c);
         if (lane == 0) {
             dn[i] = __ldg(sn + src);
+            de[i] = __ldg(se + src);
             dor[i] = __ldg(so + src);
         }
     }
@@ -1034,7 +1098,7 @@ LabelCfg label_cfg(uint32_t d_pad, uint32_t bn, size_t static_smem) {
     const size_t optin = device_info().smem_optin;
     if (optin < static_smem + 1024) return c;
     const size_t budget = optin - static_smem - 1024;
-    const size_t lists = (size_t)(CAP + 1) * EPI_THREADS * 8 + (size_t)EPI_WARPS * 32 * CAP;
+    const size_t lists = (size_t)(CAP + 1) * EPI_THREADS * 8;
     const size_t a = (size_t)PAIR_M * d_pad * 2, b = (size_t)bn * d_pad * 2;
     const uint32_t tries[][2] = {{2, 4}, {2, 3}, {2, 2}, {1, 4}, {1, 3}, {1, 2}, {1, 1}};
     for (const auto& t : tries) {
@@ -1065,6 +1129,8 @@ TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k) {
     off += align256((size_t)L.n_pad * L.d_pad * 2);
     L.pts_norm_off = off;
     off += align256((size_t)L.n_pad * 4);
+    L.pts_err_off = off;
+    off += align256((size_t)L.n_pad * 4);
     L.pts_rm_off = off;
     off += align256((size_t)n * L.d4 * 4);
     L.pts_orig_off = off;
@@ -1087,6 +1153,10 @@ TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k) {
     off += align256((size_t)n * 4);
     L.ws_slabels_off = off;
     off += align256((size_t)n * 4);
+    L.ws_res_pts_off = off;
+    off += align256((size_t)n * 4);
+    L.ws_res_cands_off = off;
+    off += align256((size_t)n * CAP * 4);
     L.ws_total = off;
     return L;
 }
@@ -1112,8 +1182,8 @@ int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, c
     count_launch();
     tc_points_convert_kernel<<<grid_for_n(n, 32, 16), 256, (size_t)d * 33 * sizeof(float), s>>>(
         P, n, d, L.d_pad, L.d4, hdr, reinterpret_cast<__half*>(b + L.pts_half_off),
-        reinterpret_cast<float*>(b + L.pts_norm_off), reinterpret_cast<float*>(b + L.pts_rm_off),
-        reinterpret_cast<uint32_t*>(b + L.pts_orig_off));
+        reinterpret_cast<float*>(b + L.pts_norm_off), reinterpret_cast<float*>(b + L.pts_err_off),
+        reinterpret_cast<float*>(b + L.pts_rm_off), reinterpret_cast<uint32_t*>(b + L.pts_orig_off));
     count_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "tc_prepare_points launch");
@@ -1131,13 +1201,15 @@ int tc_sort_points(uint64_t n, uint32_t d, uint32_t k, const void* src, void* ds
     if (e == cudaSuccess && L.n_pad > n)
         e = cudaMemsetAsync(db + L.pts_half_off + n * hrow, 0, (L.n_pad - n) * hrow, s);
     if (e == cudaSuccess && L.n_pad > n) e = cudaMemsetAsync(db + L.pts_norm_off + n * 4, 0, (L.n_pad - n) * 4, s);
+    if (e == cudaSuccess && L.n_pad > n) e = cudaMemsetAsync(db + L.pts_err_off + n * 4, 0, (L.n_pad - n) * 4, s);
     if (e != cudaSuccess) return cuda_fail(e, "tc_sort_points copy");
     if (n == 0) return CKM_OK;
     tc_sort_points_kernel<<<grid_for_n(n * 32, 256), 256, 0, s>>>(
         n, k, L.d_pad, L.d4, reinterpret_cast<const uint32_t*>(ws + L.ws_perm_off),
         reinterpret_cast<const uint32_t*>(ws + L.ws_off_off), reinterpret_cast<const uint4*>(sb + L.pts_half_off),
         reinterpret_cast<uint4*>(db + L.pts_half_off), reinterpret_cast<const float*>(sb + L.pts_norm_off),
-        reinterpret_cast<float*>(db + L.pts_norm_off), reinterpret_cast<const float4*>(sb + L.pts_rm_off),
+        reinterpret_cast<float*>(db + L.pts_norm_off), reinterpret_cast<const float*>(sb + L.pts_err_off),
+        reinterpret_cast<float*>(db + L.pts_err_off), reinterpret_cast<const float4*>(sb + L.pts_rm_off),
         reinterpret_cast<float4*>(db + L.pts_rm_off), reinterpret_cast<const uint32_t*>(sb + L.pts_orig_off),
         reinterpret_cast<uint32_t*>(db + L.pts_orig_off));
     count_launch();
@@ -1188,17 +1260,21 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
     const int cgrid = (int)((L.k_pad + 255) / 256);
     tc_centroid_stats_kernel<<<cgrid, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d4, cent_rm, cn2, it);
     count_launch();
-    tc_centroid_pack_kernel<<<cgrid, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d_pad, cn2,
-                                                  reinterpret_cast<const TcPointsHeader*>(pb), cent_half, it);
+    tc_centroid_pack_kernel<<<cgrid, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d_pad, cn2, cent_half, it);
+    count_launch();
+    tc_params_kernel<<<1, 1, 0, s>>>(a.d, L.d_pad, reinterpret_cast<const TcPointsHeader*>(pb), it);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "tc centroid launch");
 
     if (a.n > 0) {
         LabelParams prm;
         prm.norms = reinterpret_cast<const float*>(pb + L.pts_norm_off);
+        prm.errn = reinterpret_cast<const float*>(pb + L.pts_err_off);
         prm.x_rm = reinterpret_cast<const float*>(pb + L.pts_rm_off);
         prm.orig = reinterpret_cast<const uint32_t*>(pb + L.pts_orig_off);
         prm.slabels = slabels;
+        prm.res_pts = reinterpret_cast<uint32_t*>(ws + L.ws_res_pts_off);
+        prm.res_cands = reinterpret_cast<uint32_t*>(ws + L.ws_res_cands_off);
         prm.c_rm = cent_rm;
         prm.cn2 = cn2;
         prm.it = it;
@@ -1216,6 +1292,10 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
         const int rc = L.bn == 128 ? launch_label<128>(L, prm, pb + L.pts_half_off, cent_half, s)
                                    : launch_label<64>(L, prm, pb + L.pts_half_off, cent_half, s);
         if (rc) return rc;
+        tc_resolve_kernel<<<device_info().sm_count * 8, 256, 0, s>>>(prm.x_rm, cent_rm, a.d, L.d4, prm.res_pts,
+                                                                     prm.res_cands, prm.orig, it, flagged, a.labels,
+                                                                     slabels, cursor);
+        count_launch();
         tc_recheck_kernel<<<device_info().sm_count * 4, 256, (size_t)a.d * RECHECK_PTS * sizeof(float), s>>>(
             prm.x_rm, a.d, L.d4, a.k, a.centroids, flagged, prm.orig, it, a.labels, slabels, cursor);
         count_launch();

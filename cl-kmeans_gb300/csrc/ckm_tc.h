@@ -19,12 +19,14 @@ struct TcPointsHeader {
 struct TcIterDev {
     unsigned int nflagged;     // points sent to the full exact recheck
     unsigned int error;        // nonzero: a bounded device wait ran out
-    unsigned int resolved;     // points resolved among 2+ candidates in the label kernel
+    unsigned int resolved;     // points with 2+ candidates (resolved exactly after labeling)
+    unsigned int overflowed;   // points whose candidate list overflowed (part of nflagged)
     unsigned int cabs_bits;    // max |c_f| over valid centroids (float bits)
     unsigned int cmax_bits;    // upper bound of max |c| over valid centroids (float bits)
+    unsigned int fmax_bits;    // upper bound of max |fp16(c) / sc - c| over valid centroids (float bits)
     float alpha;               // score = cn2 + alpha * (fp16 dot product)
-    float t0, t1, t2, cm;      // certificate threshold T(xn) = t0 + t1 xn + t2 (xn + cm)^2
-    uint32_t reserved[54];
+    float t0, t1, te, t2, cm;  // threshold T = t0 + t1 |x| + te |e| + t2 (|x| + cm)^2, e = fp16 error of x
+    uint32_t reserved[50];
 };
 
 struct TcLayout {
@@ -34,11 +36,12 @@ struct TcLayout {
     uint32_t bn;               // clusters per chunk (TMEM columns per accumulator)
     uint64_t n_pad;            // points padded to a pair of 128-point tiles
     // prepared points (ckm_tc_points_bytes), all in the set's own point order:
-    // fp16 rows, norm bounds, FP32 rows, and the caller's index of each point
-    size_t pts_half_off, pts_norm_off, pts_rm_off, pts_orig_off, pts_total;
+    // fp16 rows, bounds of |x| and of its fp16 rounding error, FP32 rows, and
+    // the caller's index of each point
+    size_t pts_half_off, pts_norm_off, pts_err_off, pts_rm_off, pts_orig_off, pts_total;
     // per-iteration workspace (ckm_tc_workspace_bytes)
     size_t ws_cent_rm_off, ws_cent_half_off, ws_cn2_off, ws_flagged_off, ws_off_off, ws_cursor_off, ws_perm_off,
-        ws_slabels_off, ws_total;
+        ws_slabels_off, ws_res_pts_off, ws_res_cands_off, ws_total;
 };
 TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k);
 bool tc_supported(uint32_t d, uint32_t k);

@@ -37,6 +37,14 @@ int ckm_tc_sort_points(uint32_t d, uint64_t n, uint32_t k, const void* tc_points
     return tc_sort_points(n, d, k, tc_points, sorted_tc_points, workspace, (cudaStream_t)stream);
 }
 
+int ckm_tc_counters(const void* workspace, uint32_t* counters, ckm_stream_t stream) {
+    if (!workspace || !counters) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL pointer");
+    // nflagged, error, resolved, overflowed: the first four words of the workspace
+    cudaError_t e = cudaMemcpyAsync(counters, workspace, 4 * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                                    (cudaStream_t)stream);
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "ckm_tc_counters copy");
+}
+
 int ckm_tc_fused_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, const void* tc_points,
                      const float* old_centroids, float* new_centroids, uint32_t* labels, uint32_t* masses,
                      void* scratch, size_t scratch_bytes, void* workspace, size_t workspace_bytes, int mode,

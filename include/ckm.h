@@ -140,6 +140,13 @@ size_t ckm_tc_workspace_bytes(uint64_t num_points, uint32_t num_features, uint32
 int ckm_tc_supported(uint32_t num_features, uint32_t num_clusters);
 int ckm_tc_prepare_points(uint32_t num_features, uint64_t num_points, const float *points, void *tc_points,
                           size_t tc_points_bytes, ckm_stream_t stream);
+/* Diagnostics of the last ckm_tc_fused_f32 call made with `workspace`:
+ * copies to the device array counters[4] (stream-ordered) the number of
+ * points sent to the full exact recheck, the error flag, the number of
+ * points resolved among 2+ candidates in the label kernel, and the number of
+ * points whose candidate list overflowed (counted in the first value too). */
+int ckm_tc_counters(const void *workspace, uint32_t *counters, ckm_stream_t stream);
+
 /* Writes into sorted_tc_points (its own ckm_tc_points_bytes(n, d) buffer) the
  * prepared set tc_points reordered by the clusters of the last
  * ckm_tc_fused_f32 call made with `workspace` for the same set and k.  Points
