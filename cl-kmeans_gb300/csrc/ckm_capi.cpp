@@ -58,11 +58,15 @@ const DeviceInfo& device_info() {
         if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) {
             infos[dev].sm_count = p.multiProcessorCount;
             infos[dev].smem_optin = p.sharedMemPerBlockOptin;
+            infos[dev].smem_per_sm = p.sharedMemPerMultiprocessor;
+            infos[dev].smem_reserved = p.reservedSharedMemPerBlock;
             infos[dev].cc_major = p.major;
             infos[dev].cc_minor = p.minor;
         } else {
             infos[dev].sm_count = 1;
             infos[dev].smem_optin = 48 * 1024;
+            infos[dev].smem_per_sm = 48 * 1024;
+            infos[dev].smem_reserved = 0;
             infos[dev].cc_major = infos[dev].cc_minor = 0;
         }
         have[dev] = true;

@@ -44,7 +44,9 @@ uint64_t launch_count();
 // Device properties cached per device.
 struct DeviceInfo {
     int sm_count;
-    size_t smem_optin;
+    size_t smem_optin;          // per block (opt-in maximum)
+    size_t smem_per_sm;         // per multiprocessor
+    size_t smem_reserved;       // reserved by the system per block
     int cc_major, cc_minor;
 };
 const DeviceInfo& device_info();

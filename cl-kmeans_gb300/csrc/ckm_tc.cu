@@ -36,6 +36,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <mutex>
@@ -57,6 +58,7 @@ constexpr int MMA_WARP = 9;
 constexpr int LABEL_THREADS = 320;
 constexpr int CAP = 8;               // candidates kept per point in the label kernel
 constexpr int GRP = 16;              // scores per warp-uniform append test
+constexpr uint32_t CN_SMEM_MAX = 2048;  // |c|^2 of up to this many clusters is kept in shared memory
 constexpr int MAX_A_STAGES = 2;
 constexpr int MAX_B_STAGES = 4;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // bounded waits give up after 2 s
@@ -333,7 +335,7 @@ struct LabelParams {
 // minimum m and appends every cluster whose score is within T of m to its
 // candidate list in shared memory; entries that fall out of range when m
 // drops later are filtered at the end.
-template <int BN>
+template <int BN, bool CN_SMEM>
 __global__ void __launch_bounds__(LABEL_THREADS, 1)
     tc_label_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                     const LabelParams prm) {
@@ -350,6 +352,10 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
     const uint32_t a_bytes = PAIR_M * prm.d_pad * 2u, b_bytes = BN * prm.d_pad * 2u;
     const uint32_t sA = base, sB = base + prm.a_stages * a_bytes;
     float2* lists = reinterpret_cast<float2*>(smem_raw + (base - raw) + prm.a_stages * a_bytes + prm.b_stages * b_bytes);
+    // |c|^2 of all clusters in shared memory when it fits (CN_SMEM)
+    float* s_cn = reinterpret_cast<float*>(lists + (CAP + 1) * EPI_THREADS);
+    if (CN_SMEM)
+        for (uint32_t i = threadIdx.x; i < prm.chunks * BN; i += blockDim.x) s_cn[i] = __ldg(prm.cn2 + i);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t kblocks = prm.d_pad / 64u;
 
@@ -486,10 +492,10 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                 if (lane == 0) mbar_arrive(umma::smem_u32(&bar_te[u * 2 + buf]));
 
                 float s[BN];
-                const float4* cn4 = reinterpret_cast<const float4*>(prm.cn2 + (uint64_t)j * BN);
+                const float4* cn4 = reinterpret_cast<const float4*>((CN_SMEM ? s_cn : prm.cn2) + (uint64_t)j * BN);
 #pragma unroll
                 for (int i = 0; i < BN / 4; ++i) {
-                    const float4 c = __ldg(cn4 + i);
+                    const float4 c = CN_SMEM ? cn4[i] : __ldg(cn4 + i);
                     const float2 a = fma2(make_float2(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1])), al2,
                                           make_float2(c.x, c.y));
                     const float2 b = fma2(make_float2(__uint_as_float(r[4 * i + 2]), __uint_as_float(r[4 * i + 3])),
@@ -1059,15 +1065,23 @@ int grid_for_n(uint64_t n, int block, int per_sm = 16) {
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// Shape of the label kernel: clusters per chunk and CTAs per SM.  One CTA
+// per SM holds all 512 tensor-memory columns (two tiles x two buffers x 128
+// clusters); with d_pad = 256 the chunks are 64 clusters to fit shared
+// memory.  (Two CTAs per SM with 64-cluster chunks measured slower: one
+// centroid stage each and twice the centroid traffic.)
+uint32_t label_bn(uint32_t d_pad) { return d_pad <= 192 ? 128u : 64u; }
+uint32_t label_ctas_per_sm(uint32_t) { return 1u; }
+
 // Pipeline depth of the label kernel for a shape: two pair stages when they
 // fit, then as many centroid stages as fit (at least one of each).
 struct LabelCfg {
-    uint32_t a_stages, b_stages;
+    uint32_t a_stages, b_stages, ctas_per_sm;
     size_t smem;
     bool ok;
 };
 
-template <int BN>
+template <int BN, bool CN_SMEM>
 int label_static_smem(size_t* out) {
     static size_t cached[64] = {0};
     static bool have[64] = {false};
@@ -1080,9 +1094,9 @@ int label_static_smem(size_t* out) {
         return CKM_OK;
     }
     cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, tc_label_kernel<BN>);
+    cudaError_t e = cudaFuncGetAttributes(&fa, tc_label_kernel<BN, CN_SMEM>);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(tc_label)");
-    e = cudaFuncSetAttribute(tc_label_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(tc_label_kernel<BN, CN_SMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(device_info().smem_optin - fa.sharedSizeBytes));
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(tc_label)");
     if (dev >= 0 && dev < 64) {
@@ -1093,12 +1107,14 @@ int label_static_smem(size_t* out) {
     return CKM_OK;
 }
 
-LabelCfg label_cfg(uint32_t d_pad, uint32_t bn, size_t static_smem) {
-    LabelCfg c{0, 0, 0, false};
-    const size_t optin = device_info().smem_optin;
-    if (optin < static_smem + 1024) return c;
-    const size_t budget = optin - static_smem - 1024;
-    const size_t lists = (size_t)(CAP + 1) * EPI_THREADS * 8;
+LabelCfg label_cfg(uint32_t d_pad, uint32_t bn, uint32_t ctas, size_t static_smem, size_t extra = 0) {
+    LabelCfg c{0, 0, ctas, 0, false};
+    const DeviceInfo& di = device_info();
+    const size_t per_cta = di.smem_per_sm / ctas;  // including the system's reservation
+    const size_t limit = std::min(di.smem_optin, per_cta > di.smem_reserved ? per_cta - di.smem_reserved : 0);
+    if (limit < static_smem + 1024) return c;
+    const size_t budget = limit - static_smem - 1024;  // 1024: alignment of the swizzled tiles
+    const size_t lists = (size_t)(CAP + 1) * EPI_THREADS * 8 + extra;
     const size_t a = (size_t)PAIR_M * d_pad * 2, b = (size_t)bn * d_pad * 2;
     const uint32_t tries[][2] = {{2, 4}, {2, 3}, {2, 2}, {1, 4}, {1, 3}, {1, 2}, {1, 1}};
     for (const auto& t : tries) {
@@ -1107,7 +1123,11 @@ LabelCfg label_cfg(uint32_t d_pad, uint32_t bn, size_t static_smem) {
             c.a_stages = t[0];
             c.b_stages = t[1];
             c.smem = need + 1024;
-            if (c.smem < 120 * 1024) c.smem = 120 * 1024;  // one CTA per SM: it allocates all TMEM columns
+            // no more than `ctas` CTAs per SM: together they own all the
+            // tensor-memory columns
+            const size_t floor_smem = di.smem_per_sm / (ctas + 1) + 1;
+            if (c.smem + static_smem + di.smem_reserved < floor_smem)
+                c.smem = floor_smem - static_smem - di.smem_reserved;
             c.ok = true;
             return c;
         }
@@ -1121,7 +1141,7 @@ TcLayout tc_layout(uint64_t n, uint32_t d, uint32_t k) {
     TcLayout L;
     L.d_pad = (d + 63) / 64 * 64;
     L.d4 = (d + 3) / 4 * 4;
-    L.bn = L.d_pad <= 192 ? 128u : 64u;
+    L.bn = label_bn(L.d_pad);
     L.k_pad = (k + L.bn - 1) / L.bn * L.bn;
     L.n_pad = ((n > 0 ? n : 1) + PAIR_M - 1) / PAIR_M * PAIR_M;
     size_t off = 256;  // TcPointsHeader
@@ -1167,7 +1187,7 @@ bool tc_supported(uint32_t d, uint32_t k) {
     const uint32_t d_pad = (d + 63) / 64 * 64;
     if (d_pad > 256) return false;
     // the label kernel's static shared memory is under 1 KB
-    return label_cfg(d_pad, d_pad <= 192 ? 128u : 64u, 1024).ok;
+    return label_cfg(d_pad, label_bn(d_pad), label_ctas_per_sm(d_pad), 1024, CN_SMEM_MAX * sizeof(float)).ok;
 }
 
 int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, cudaStream_t s) {
@@ -1217,13 +1237,14 @@ int tc_sort_points(uint64_t n, uint32_t d, uint32_t k, const void* src, void* ds
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "tc_sort_points launch");
 }
 
-template <int BN>
+template <int BN, bool CN_SMEM>
 static int launch_label(const TcLayout& L, const LabelParams& prm, const void* pts_half, const void* cent_half,
                         cudaStream_t s) {
     size_t st = 0;
-    int rc = label_static_smem<BN>(&st);
+    int rc = label_static_smem<BN, CN_SMEM>(&st);
     if (rc) return rc;
-    const LabelCfg cfg = label_cfg(L.d_pad, BN, st);
+    const LabelCfg cfg =
+        label_cfg(L.d_pad, BN, label_ctas_per_sm(L.d_pad), st, CN_SMEM ? (size_t)L.k_pad * sizeof(float) : 0);
     if (!cfg.ok) return fail(CKM_ERR_UNSUPPORTED, "tensor-core label kernel: shared memory too small");
     CUtensorMap tm_a, tm_b;
     if ((rc = make_map(&tm_a, pts_half, L.n_pad, L.d_pad, PAIR_M))) return rc;
@@ -1231,11 +1252,22 @@ static int launch_label(const TcLayout& L, const LabelParams& prm, const void* p
     LabelParams p = prm;
     p.a_stages = cfg.a_stages;
     p.b_stages = cfg.b_stages;
-    const uint32_t grid = p.num_pairs < (uint32_t)device_info().sm_count ? p.num_pairs : (uint32_t)device_info().sm_count;
-    tc_label_kernel<BN><<<grid, LABEL_THREADS, cfg.smem, s>>>(tm_a, tm_b, p);
+    const uint32_t slots = (uint32_t)device_info().sm_count * cfg.ctas_per_sm;
+    const uint32_t grid = p.num_pairs < slots ? p.num_pairs : slots;
+    tc_label_kernel<BN, CN_SMEM><<<grid, LABEL_THREADS, cfg.smem, s>>>(tm_a, tm_b, p);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "tc_label launch");
+}
+
+static int launch_label_for(const TcLayout& L, const LabelParams& prm, const void* pts_half, const void* cent_half,
+                            cudaStream_t s) {
+    const bool cn_smem = L.k_pad <= CN_SMEM_MAX;
+    if (L.bn == 128)
+        return cn_smem ? launch_label<128, true>(L, prm, pts_half, cent_half, s)
+                       : launch_label<128, false>(L, prm, pts_half, cent_half, s);
+    return cn_smem ? launch_label<64, true>(L, prm, pts_half, cent_half, s)
+                   : launch_label<64, false>(L, prm, pts_half, cent_half, s);
 }
 
 int tc_iteration(const TcArgs& a, cudaStream_t s) {
@@ -1289,8 +1321,7 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
         prm.chunks = L.k_pad / L.bn;
         prm.num_pairs = (uint32_t)(L.n_pad / PAIR_M);
         prm.a_stages = prm.b_stages = 1;
-        const int rc = L.bn == 128 ? launch_label<128>(L, prm, pb + L.pts_half_off, cent_half, s)
-                                   : launch_label<64>(L, prm, pb + L.pts_half_off, cent_half, s);
+        const int rc = launch_label_for(L, prm, pb + L.pts_half_off, cent_half, s);
         if (rc) return rc;
         tc_resolve_kernel<<<device_info().sm_count * 8, 256, 0, s>>>(prm.x_rm, cent_rm, a.d, L.d4, prm.res_pts,
                                                                      prm.res_cands, prm.orig, it, flagged, a.labels,
