@@ -317,7 +317,7 @@ struct LabelParams {
     const float* cn2;            // |c|^2 [k_pad]
     TcIterDev* it;
     uint32_t* labels;            // caller's order
-    uint32_t* slabels;           // the set's order
+    uint32_t* slabels;           // the set's order (on entry: the previous call's, read for the chunk order)
     uint32_t* counts;            // points per label in this call
     uint32_t* flagged;           // points for the full recheck
     uint32_t* res_pts;           // points with 2+ candidates (tc_resolve_kernel)
@@ -325,6 +325,21 @@ struct LabelParams {
     uint64_t n;
     uint32_t d, d4, d_pad, k, chunks, num_pairs, a_stages, b_stages;
 };
+
+// First chunk of pair q: the chunk holding the previous label of the pair's
+// middle point.  In a cluster-ordered set most points of the pair share that
+// label, so the running minimum is (nearly) final after the first chunk and
+// later chunks append only true candidates.  Any value gives a valid order
+// (the chunks are visited cyclically from it), so an uninitialised or stale
+// label only costs time.  The label is read before this call writes it: the
+// pair's epilogue writes its labels after all three roles have read it.
+template <int BN>
+__device__ __forceinline__ uint32_t home_chunk(const LabelParams& prm, uint32_t q) {
+    uint64_t pm = (uint64_t)q * PAIR_M + TILE_M;
+    if (pm >= prm.n) pm = (uint64_t)q * PAIR_M;
+    const uint32_t lab = *(volatile const uint32_t*)(prm.slabels + pm);
+    return lab < prm.k ? (lab / BN) % prm.chunks : 0u;
+}
 
 // One CTA per SM, looping over pairs of 128-point tiles.  Warp 8 (one lane)
 // streams the pair's fp16 rows and the centroid chunks by TMA; warp 9 (one
@@ -394,12 +409,14 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                     umma::tma_load_2d(sA + sa * a_bytes + kb * (PAIR_M * 128u), &tm_a, (int)(kb * 64),
                                       (int)(q * PAIR_M), umma::smem_u32(&bar_af[sa]));
                 ++ia;
+                const uint32_t j0 = home_chunk<BN>(prm, q);
                 for (uint32_t j = 0; j < prm.chunks; ++j) {
+                    const uint32_t jj = j0 + j < prm.chunks ? j0 + j : j0 + j - prm.chunks;
                     const uint32_t sb = ib % prm.b_stages, pb = (ib / prm.b_stages) & 1u;
                     if (!(ok = wait_phase(umma::smem_u32(&bar_be[sb]), pb ^ 1u, abort_flag))) break;
                     umma::mbar_arrive_expect_tx(umma::smem_u32(&bar_bf[sb]), b_bytes);
                     for (uint32_t kb = 0; kb < kblocks; ++kb)
-                        umma::tma_load_2d(sB + sb * b_bytes + kb * (BN * 128u), &tm_b, (int)(kb * 64), (int)(j * BN),
+                        umma::tma_load_2d(sB + sb * b_bytes + kb * (BN * 128u), &tm_b, (int)(kb * 64), (int)(jj * BN),
                                           umma::smem_u32(&bar_bf[sb]));
                     ++ib;
                 }
@@ -471,7 +488,9 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
             float m = INF;
             uint32_t cnt = 0;
             bool ovf = false;
+            const uint32_t j0 = home_chunk<BN>(prm, q);
             for (uint32_t j = 0; j < prm.chunks; ++j, ++ic) {
+                const uint32_t jj = j0 + j < prm.chunks ? j0 + j : j0 + j - prm.chunks;
                 const uint32_t buf = ic & 1u, pt = (ic >> 1) & 1u;
                 int ok = 1;
                 if (lane == 0) ok = wait_phase(umma::smem_u32(&bar_tf[u * 2 + buf]), pt, abort_flag);
@@ -492,7 +511,7 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                 if (lane == 0) mbar_arrive(umma::smem_u32(&bar_te[u * 2 + buf]));
 
                 float s[BN];
-                const float4* cn4 = reinterpret_cast<const float4*>((CN_SMEM ? s_cn : prm.cn2) + (uint64_t)j * BN);
+                const float4* cn4 = reinterpret_cast<const float4*>((CN_SMEM ? s_cn : prm.cn2) + (uint64_t)jj * BN);
 #pragma unroll
                 for (int i = 0; i < BN / 4; ++i) {
                     const float4 c = CN_SMEM ? cn4[i] : __ldg(cn4 + i);
@@ -522,7 +541,7 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                 const float cut = m + T;
                 // appends: a group is scanned only when one of the warp's points
                 // has a score in range there (a warp-uniform branch)
-                const uint32_t cbase = j * BN;
+                const uint32_t cbase = jj * BN;
 #pragma unroll
                 for (int g = 0; g < BN / GRP; ++g) {
                     if (__any_sync(0xffffffffu, valid && gm[g] <= cut)) {
@@ -889,15 +908,18 @@ __device__ __forceinline__ void two_sum_add(float& hi, float& lo, float v) {
 
 // Per warp a slice of SEG positions of the label order: the rows of the
 // points of one cluster are contiguous there, so each lane accumulates its
-// features (f = lane + 32 j) as float pairs and merges them into the FP64
-// sums [d][k] only where the cluster changes.
+// features (float4 q = lane + 32 j of the row: features 4q..4q+3) as float
+// pairs and merges them into the FP64 sums [d][k] only where the cluster
+// changes.  ROWS rows are loaded before they are added, to keep loads in flight.
 constexpr uint32_t SEG = 512;
+constexpr int ROWS = 8;
 template <int J>
 __global__ void __launch_bounds__(256) tc_segment_sum_kernel(const float* __restrict__ x_rm, uint32_t d, uint32_t d4,
                                                              uint64_t n, uint32_t k, const uint32_t* __restrict__ perm,
                                                              const uint32_t* __restrict__ off,
                                                              double* __restrict__ sums) {
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t q4 = d4 / 4;  // float4 per row
     const uint64_t wid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     // positions past off[k] belong to no cluster (only after a failed labeling)
@@ -912,39 +934,43 @@ __global__ void __launch_bounds__(256) tc_segment_sum_kernel(const float* __rest
         }
         uint32_t c = lo;
         uint64_t end = __ldg(off + c + 1);
-        float ah[J], al[J];
+        float ah[J][4], al[J][4];
 #pragma unroll
-        for (int j = 0; j < J; ++j) ah[j] = al[j] = 0.0f;
+        for (int j = 0; j < J; ++j)
+#pragma unroll
+            for (int t = 0; t < 4; ++t) ah[j][t] = al[j][t] = 0.0f;
         bool any = false;
         auto flush = [&]() {
             if (any) {
 #pragma unroll
-                for (int j = 0; j < J; ++j) {
-                    const uint32_t f = lane + 32u * j;
-                    if (f < d) atomicAdd(&sums[(uint64_t)f * k + c], (double)ah[j] + (double)al[j]);
-                    ah[j] = al[j] = 0.0f;
-                }
+                for (int j = 0; j < J; ++j)
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const uint32_t f = 4u * (lane + 32u * j) + t;
+                        if (f < d) atomicAdd(&sums[(uint64_t)f * k + c], (double)ah[j][t] + (double)al[j][t]);
+                        ah[j][t] = al[j][t] = 0.0f;
+                    }
             }
             any = false;
         };
         for (uint64_t b = s0; b < s1; b += 32) {
             const uint32_t cntq = (uint32_t)(s1 - b < 32 ? s1 - b : 32);
             const uint32_t myp = lane < cntq ? __ldg(perm + b + lane) : 0u;
-            for (uint32_t i = 0; i < cntq; i += 4) {
-                float v[4][J];
+            for (uint32_t i = 0; i < cntq; i += ROWS) {
+                float4 v[ROWS][J];
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
+                for (int r = 0; r < ROWS; ++r) {
                     const uint32_t pr = __shfl_sync(0xffffffffu, myp, (i + r) & 31);
                     const bool ok = i + r < cntq && pr < n;
-                    const float* row = x_rm + (uint64_t)(ok ? pr : 0u) * d4;
+                    const float4* row = reinterpret_cast<const float4*>(x_rm + (uint64_t)(ok ? pr : 0u) * d4);
 #pragma unroll
                     for (int j = 0; j < J; ++j) {
-                        const uint32_t f = lane + 32u * j;
-                        v[r][j] = (ok && f < d) ? __ldg(row + f) : 0.0f;
+                        const uint32_t qq = lane + 32u * j;
+                        v[r][j] = (ok && qq < q4) ? __ldg(row + qq) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     }
                 }
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
+                for (int r = 0; r < ROWS; ++r) {
                     if (i + r >= cntq) break;
                     const uint64_t qpos = b + i + r;
                     while (qpos >= end) {  // cluster boundary (empty clusters are skipped)
@@ -953,7 +979,12 @@ __global__ void __launch_bounds__(256) tc_segment_sum_kernel(const float* __rest
                         end = __ldg(off + c + 1);
                     }
 #pragma unroll
-                    for (int j = 0; j < J; ++j) two_sum_add(ah[j], al[j], v[r][j]);
+                    for (int j = 0; j < J; ++j) {
+                        two_sum_add(ah[j][0], al[j][0], v[r][j].x);
+                        two_sum_add(ah[j][1], al[j][1], v[r][j].y);
+                        two_sum_add(ah[j][2], al[j][2], v[r][j].z);
+                        two_sum_add(ah[j][3], al[j][3], v[r][j].w);
+                    }
                     any = true;
                 }
             }
@@ -1347,14 +1378,10 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
         const uint64_t warps = (a.n + SEG - 1) / SEG;
         const int sgrid = grid_for_n(warps * 32, 256);
         const float* x_rm = reinterpret_cast<const float*>(pb + L.pts_rm_off);
-        if (a.d <= 32)
+        if (L.d4 <= 128)
             tc_segment_sum_kernel<1><<<sgrid, 256, 0, s>>>(x_rm, a.d, L.d4, a.n, a.k, perm, off, a.scratch.sums);
-        else if (a.d <= 64)
-            tc_segment_sum_kernel<2><<<sgrid, 256, 0, s>>>(x_rm, a.d, L.d4, a.n, a.k, perm, off, a.scratch.sums);
-        else if (a.d <= 128)
-            tc_segment_sum_kernel<4><<<sgrid, 256, 0, s>>>(x_rm, a.d, L.d4, a.n, a.k, perm, off, a.scratch.sums);
         else
-            tc_segment_sum_kernel<8><<<sgrid, 256, 0, s>>>(x_rm, a.d, L.d4, a.n, a.k, perm, off, a.scratch.sums);
+            tc_segment_sum_kernel<2><<<sgrid, 256, 0, s>>>(x_rm, a.d, L.d4, a.n, a.k, perm, off, a.scratch.sums);
         count_launch();
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "tc update launch");
