@@ -60,6 +60,8 @@ class RunConfig(ctypes.Structure):
         ("device", ctypes.c_int),
         ("device_budget_bytes", ctypes.c_uint64),
         ("chunk_bytes", ctypes.c_uint64),
+        ("converge", ctypes.c_int),
+        ("tolerance", ctypes.c_double),
     ]
 
 
@@ -71,6 +73,8 @@ class RunInfo(ctypes.Structure):
         ("d2h_bytes", ctypes.c_uint64),
         ("kernel_launches", ctypes.c_uint64),
         ("iterations", ctypes.c_uint32),
+        ("converged", ctypes.c_uint32),
+        ("last_shift", ctypes.c_float),
     ]
 
 
@@ -236,9 +240,11 @@ def launch_count():
 def kmeans_run(points, d, k, iterations, centroids, pipeline="single_stage", fused_strategy="feature_sum",
                labeling_strategy="unroll_vector", mass_update_strategy="part_local",
                centroid_update_strategy="feature_sum", device=0, device_budget_bytes=0, chunk_bytes=0,
-               masses=None, labels=None):
+               masses=None, labels=None, converge=False, tolerance=0.0):
     """AbstractKmeans::operator() over HOST numpy arrays (column-major flat
-    points and centroids).  Returns (centroids, masses, labels, RunInfo)."""
+    points and centroids).  converge: stop once the relative centroid shift
+    falls below tolerance (default 1e-4).  Returns (centroids, masses,
+    labels, RunInfo)."""
     import numpy as np
     f64 = points.dtype == np.float64
     P = np.ascontiguousarray(points, np.float64 if f64 else np.float32)
@@ -249,7 +255,7 @@ def kmeans_run(points, d, k, iterations, centroids, pipeline="single_stage", fus
     Lb = np.zeros(n, it) if labels is None else labels
     cfg = RunConfig(pipeline.encode(), fused_strategy.encode(), labeling_strategy.encode(),
                     mass_update_strategy.encode(), centroid_update_strategy.encode(), device,
-                    device_budget_bytes, chunk_bytes)
+                    device_budget_bytes, chunk_bytes, 1 if converge else 0, float(tolerance))
     info = RunInfo()
     fn = lib().ckm_kmeans_run_f64 if f64 else lib().ckm_kmeans_run_f32
     check(fn(ctypes.byref(cfg), iterations, d, n, k, P.ctypes.data, C.ctypes.data, M.ctypes.data,
@@ -459,6 +465,7 @@ class MixtureSpec(ctypes.Structure):
 
 
 EXPORTS.append("ckm_generate_mixture_ex_f32")
+EXPORTS += ["ckm_centroid_shift_f32", "ckm_centroid_shift_f64"]
 
 
 def generate_mixture_ex(points, n, d, blobs, seed, center=("uniform", -10.0, 10.0), sigma=("uniform", 1.0, 1.0),

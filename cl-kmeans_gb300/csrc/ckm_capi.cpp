@@ -254,6 +254,18 @@ int ckm_centroid_update_f64(uint32_t d, uint64_t n, uint32_t k, const double* po
     return launch_generic_f64(a, Pass::SumsOnly, (cudaStream_t)stream);
 }
 
+int ckm_centroid_shift_f32(uint32_t d, uint32_t k, const float* old_c, const float* new_c, float* shift,
+                           ckm_stream_t stream) {
+    if (d == 0 || k == 0 || !old_c || !new_c || !shift) return fail(CKM_ERR_INVALID_ARGUMENT, "bad shift arguments");
+    return launch_shift_f32((uint64_t)k * d, old_c, new_c, shift, (cudaStream_t)stream);
+}
+
+int ckm_centroid_shift_f64(uint32_t d, uint32_t k, const double* old_c, const double* new_c, float* shift,
+                           ckm_stream_t stream) {
+    if (d == 0 || k == 0 || !old_c || !new_c || !shift) return fail(CKM_ERR_INVALID_ARGUMENT, "bad shift arguments");
+    return launch_shift_f64((uint64_t)k * d, old_c, new_c, shift, (cudaStream_t)stream);
+}
+
 int ckm_matrix_divide_row_f32(uint32_t d, uint32_t k, float* m, const uint32_t* masses, ckm_stream_t stream) {
     if (d == 0 || k == 0 || !m || !masses) return fail(CKM_ERR_INVALID_ARGUMENT, "bad divide arguments");
     return launch_divide_f32(d, k, m, masses, (cudaStream_t)stream);

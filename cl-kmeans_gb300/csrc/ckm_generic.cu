@@ -410,6 +410,50 @@ int launch_mass_u64(uint64_t n, uint32_t k, const uint64_t* labels, uint64_t* ma
     return launch_mass_t<uint64_t, unsigned long long>(n, k, labels, reinterpret_cast<unsigned long long*>(masses), s);
 }
 
+// Relative centroid shift: max |new - old| over max |old| (NaN entries, the
+// empty clusters, are skipped by fmaxf).  One CTA.
+template <typename T>
+__global__ void __launch_bounds__(1024) shift_kernel(uint64_t kd, const T* __restrict__ old_c,
+                                                     const T* __restrict__ new_c, float* __restrict__ out) {
+    __shared__ float s_a[32], s_b[32];
+    float a = 0.0f, b = 0.0f;
+    for (uint64_t e = threadIdx.x; e < kd; e += blockDim.x) {
+        const T o = old_c[e];
+        a = fmaxf(a, (float)fabs((double)new_c[e] - (double)o));
+        b = fmaxf(b, (float)fabs((double)o));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_a[threadIdx.x >> 5] = a;
+        s_b[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned w = 1; w < blockDim.x / 32; ++w) {
+            a = fmaxf(a, s_a[w]);
+            b = fmaxf(b, s_b[w]);
+        }
+        out[0] = a / fmaxf(b, 1e-30f);
+    }
+}
+
+int launch_shift_f32(uint64_t kd, const float* o, const float* n, float* out, cudaStream_t s) {
+    shift_kernel<float><<<1, 1024, 0, s>>>(kd, o, n, out);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "shift launch");
+}
+
+int launch_shift_f64(uint64_t kd, const double* o, const double* n, float* out, cudaStream_t s) {
+    shift_kernel<double><<<1, 1024, 0, s>>>(kd, o, n, out);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "shift launch");
+}
+
 int launch_divide_f32(uint32_t d, uint32_t k, float* m, const uint32_t* masses, cudaStream_t s) {
     divide_kernel<float, uint32_t><<<grid_for((uint64_t)k * d, 256), 256, 0, s>>>(d, k, m, masses);
     count_launch();

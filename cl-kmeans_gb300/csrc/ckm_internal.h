@@ -90,6 +90,8 @@ int launch_finalize_f64(uint32_t d, uint32_t k, double* c, uint64_t* m, ScratchV
                         cudaStream_t s);
 int launch_mass_u32(uint64_t n, uint32_t k, const uint32_t* labels, uint32_t* masses, cudaStream_t s);
 int launch_mass_u64(uint64_t n, uint32_t k, const uint64_t* labels, uint64_t* masses, cudaStream_t s);
+int launch_shift_f32(uint64_t kd, const float* o, const float* n, float* out, cudaStream_t s);
+int launch_shift_f64(uint64_t kd, const double* o, const double* n, float* out, cudaStream_t s);
 int launch_divide_f32(uint32_t d, uint32_t k, float* m, const uint32_t* masses, cudaStream_t s);
 int launch_divide_f64(uint32_t d, uint32_t k, double* m, const uint64_t* masses, cudaStream_t s);
 template <typename T>

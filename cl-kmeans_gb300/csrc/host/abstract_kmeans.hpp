@@ -45,6 +45,13 @@ public:
     virtual ~AbstractKmeans() {}
 
     virtual void set_max_iterations(size_t i) { this->max_iterations = i; }
+    // `kmeans.converge`: stop once the relative centroid shift of an
+    // iteration (max |new - old| / max |old|) is below the tolerance.
+    virtual void set_converge(bool c) { this->converge = c; }
+    virtual void set_tolerance(double t) { this->tolerance = t > 0.0 ? t : 1e-4; }
+    size_t iterations_done() const { return this->done_iterations; }
+    bool did_converge() const { return this->converged; }
+    float last_shift() const { return this->shift; }
 
     virtual void set_points(std::shared_ptr<const std::vector<PointT>> p) {
         this->host_points = p;
@@ -121,7 +128,28 @@ protected:
     MassT* out_masses() const { return raw_masses ? raw_masses : host_masses->data(); }
     LabelT* out_labels() const { return raw_labels ? raw_labels : host_labels->data(); }
 
+    // The drivers call this after each iteration; it returns true when the
+    // loop should stop (a converging run whose shift fell below tolerance).
+    template <typename Probe, typename P>
+    bool after_iteration(size_t it, Probe& probe, uint32_t d, uint32_t k, const P* old_c, const P* new_c, Stream& q) {
+        this->done_iterations = it + 1;
+        if (!this->converge) return false;
+        this->converged = probe.converged(d, k, old_c, new_c, this->tolerance, q);
+        this->shift = probe.last();
+        return this->converged;
+    }
+    void reset_progress() {
+        this->done_iterations = 0;
+        this->converged = false;
+        this->shift = 0.0f;
+    }
+
     size_t max_iterations;
+    bool converge = false;
+    double tolerance = 1e-4;
+    size_t done_iterations = 0;
+    bool converged = false;
+    float shift = 0.0f;
     size_t num_features;
     size_t num_points;
     size_t num_clusters;

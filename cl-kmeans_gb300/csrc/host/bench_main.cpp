@@ -272,6 +272,8 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
             s->set_labeler(ll);
             s->set_mass_updater(mu);
             s->set_centroid_updater(cu);
+            s->set_converge(km.converge);
+            s->set_tolerance(gb.tolerance);
             kmeans = [s](size_t a, size_t b, std::shared_ptr<const std::vector<P>> c, std::shared_ptr<std::vector<P>> e,
                          std::shared_ptr<std::vector<M>> f, std::shared_ptr<std::vector<L>> g) {
                 return (*s)(a, b, c, e, f, g);
@@ -285,6 +287,8 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
             s->set_labeler(ll);
             s->set_mass_updater(mu);
             s->set_centroid_updater(cu);
+            s->set_converge(km.converge);
+            s->set_tolerance(gb.tolerance);
             kmeans = [s](size_t a, size_t b, std::shared_ptr<const std::vector<P>> c, std::shared_ptr<std::vector<P>> e,
                          std::shared_ptr<std::vector<M>> f, std::shared_ptr<std::vector<L>> g) {
                 return (*s)(a, b, c, e, f, g);
@@ -302,6 +306,8 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
             auto s = std::make_shared<KmeansSingleStage<P, L, M>>();
             s->set_queue(Stream::create((int)fu.device));
             s->set_fused(fu);
+            s->set_converge(km.converge);
+            s->set_tolerance(gb.tolerance);
             kmeans = [s](size_t a, size_t b, std::shared_ptr<const std::vector<P>> c, std::shared_ptr<std::vector<P>> e,
                          std::shared_ptr<std::vector<M>> f, std::shared_ptr<std::vector<L>> g) {
                 return (*s)(a, b, c, e, f, g);
@@ -313,6 +319,8 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
             bo.chunk_bytes = (uint64_t)gb.chunk_mib << 20;
             s->set_options(bo);
             s->set_fused(fu);
+            s->set_converge(km.converge);
+            s->set_tolerance(gb.tolerance);
             kmeans = [s](size_t a, size_t b, std::shared_ptr<const std::vector<P>> c, std::shared_ptr<std::vector<P>> e,
                          std::shared_ptr<std::vector<M>> f, std::shared_ptr<std::vector<L>> g) {
                 return (*s)(a, b, c, e, f, g);
@@ -426,7 +434,8 @@ int print_config(const ConfigurationParser& c) {
     print_sizes("kmeans.fused.local_size", f.local_size);
     std::cout << "kmeans.fused.vector_length=" << f.vector_length << "\n";
     std::cout << "kmeans.gb300.device_budget_mib=" << g.device_budget_mib << "\nkmeans.gb300.chunk_mib=" << g.chunk_mib
-              << "\nkmeans.gb300.copy_streams=" << g.copy_streams << "\nkmeans.gb300.graphs=" << g.graphs << "\n";
+              << "\nkmeans.gb300.copy_streams=" << g.copy_streams << "\nkmeans.gb300.graphs=" << g.graphs
+              << "\nkmeans.gb300.tolerance=" << g.tolerance << "\n";
     return 1;
 }
 

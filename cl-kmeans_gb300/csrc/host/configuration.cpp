@@ -43,6 +43,7 @@ const std::map<std::string, Kind>& known_keys() {
         m["kmeans.gb300.chunk_mib"] = Kind::Size;
         m["kmeans.gb300.copy_streams"] = Kind::Size;
         m["kmeans.gb300.graphs"] = Kind::Bool;
+        m["kmeans.gb300.tolerance"] = Kind::String;  // a positive real, checked by to_real
         return m;
     }();
     return keys;
@@ -67,6 +68,19 @@ size_t to_size(const std::string& key, const std::string& v) {
     }
     if (pos != t.size()) throw std::invalid_argument("invalid value for " + key + ": '" + v + "'");
     return (size_t)r;
+}
+
+double to_real(const std::string& key, const std::string& v) {
+    std::string t = trim(v);
+    size_t pos = 0;
+    double r = 0.0;
+    try {
+        r = std::stod(t, &pos);
+    } catch (...) {
+        throw std::invalid_argument("invalid value for " + key + ": '" + v + "'");
+    }
+    if (pos != t.size() || !(r > 0.0)) throw std::invalid_argument("invalid value for " + key + ": '" + v + "'");
+    return r;
 }
 
 // Boost program_options accepts true/false, yes/no, on/off, 1/0.
@@ -228,6 +242,7 @@ Gb300Configuration ConfigurationParser::get_gb300_configuration() const {
         else if (o.first == "kmeans.gb300.chunk_mib") c.chunk_mib = to_size(o.first, v);
         else if (o.first == "kmeans.gb300.copy_streams") c.copy_streams = to_size(o.first, v);
         else if (o.first == "kmeans.gb300.graphs") c.graphs = to_bool(o.first, v);
+        else if (o.first == "kmeans.gb300.tolerance") c.tolerance = to_real(o.first, v);
     }
     return c;
 }

@@ -75,6 +75,7 @@ struct Gb300Configuration {
     size_t chunk_mib = 0;          // buffered pipelines: points MiB per chunk (0 = automatic)
     size_t copy_streams = 2;       // buffered pipelines: host<->device copy streams
     bool graphs = true;            // capture the iteration loop in a CUDA graph where possible
+    double tolerance = 1e-4;       // kmeans.converge: stop below this relative centroid shift
 };
 
 class ConfigurationParser {

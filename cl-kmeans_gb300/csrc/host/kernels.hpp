@@ -41,6 +41,9 @@ struct Api<float, uint32_t, uint32_t> {
     static int divide(uint32_t d, uint32_t k, float* c, const uint32_t* m, cudaStream_t q) {
         return ckm_matrix_divide_row_f32(d, k, c, m, (ckm_stream_t)q);
     }
+    static int shift(uint32_t d, uint32_t k, const float* o, const float* n, float* out, cudaStream_t q) {
+        return ckm_centroid_shift_f32(d, k, o, n, out, (ckm_stream_t)q);
+    }
     static int add_points(uint64_t n, float* a, const float* b, cudaStream_t q) {
         return ckm_matrix_add_f32(n, a, b, (ckm_stream_t)q);
     }
@@ -71,6 +74,9 @@ struct Api<double, uint64_t, uint64_t> {
     }
     static int divide(uint32_t d, uint32_t k, double* c, const uint64_t* m, cudaStream_t q) {
         return ckm_matrix_divide_row_f64(d, k, c, m, (ckm_stream_t)q);
+    }
+    static int shift(uint32_t d, uint32_t k, const double* o, const double* n, float* out, cudaStream_t q) {
+        return ckm_centroid_shift_f64(d, k, o, n, out, (ckm_stream_t)q);
     }
     static int add_points(uint64_t n, double* a, const double* b, cudaStream_t q) {
         return ckm_matrix_add_f64(n, a, b, (ckm_stream_t)q);
@@ -297,6 +303,41 @@ public:
 
 private:
     BinaryOp op_ = Divide;
+};
+
+// The `kmeans.converge` test between iterations: the relative centroid
+// shift (ckm_centroid_shift_*) is computed on the device and read back
+// through a pinned word, which synchronises the stream once per iteration
+// (only in converging runs).
+template <typename PointT, typename LabelT, typename MassT>
+class ConvergenceProbe {
+public:
+    ConvergenceProbe() = default;
+    ConvergenceProbe(const ConvergenceProbe&) = delete;
+    ConvergenceProbe& operator=(const ConvergenceProbe&) = delete;
+    ~ConvergenceProbe() {
+        if (dev_) cudaFree(dev_);
+        if (host_) cudaFreeHost(host_);
+    }
+
+    // true when the shift from old_c to new_c is below tolerance
+    bool converged(uint32_t d, uint32_t k, const PointT* old_c, const PointT* new_c, double tolerance, Stream& q) {
+        if (!dev_) {
+            cuda_check(cudaMalloc(&dev_, sizeof(float)), "cudaMalloc(shift)");
+            cuda_check(cudaMallocHost(&host_, sizeof(float)), "cudaMallocHost(shift)");
+        }
+        ckm_check(Api<PointT, LabelT, MassT>::shift(d, k, old_c, new_c, dev_, q.get()), "ckm_centroid_shift");
+        cuda_check(cudaMemcpyAsync(host_, dev_, sizeof(float), cudaMemcpyDeviceToHost, q.get()), "shift copy");
+        q.finish();
+        last_ = *host_;
+        return last_ < tolerance;
+    }
+    float last() const { return last_; }
+
+private:
+    float* dev_ = nullptr;
+    float* host_ = nullptr;
+    float last_ = 0.0f;
 };
 
 }  // namespace Clustering

@@ -277,8 +277,11 @@ protected:
 
         Timer::Timer total_timer;
         total_timer.start();
+        this->reset_progress();
         for (uint32_t it = 0; it < this->max_iterations; ++it) {
-            const bool last = it + 1 == this->max_iterations;
+            // labels of streamed chunks go back to the host in the last
+            // iteration; a converging run may stop after any iteration
+            const bool last = it + 1 == this->max_iterations || this->converge;
             masses_.fill_zero_async(queue_);
             auto& dp = this->measurement->add_datapoint((int)it).set_name("ChunkLoop");
             Event& ev = dp.add_event(queue_);
@@ -294,6 +297,8 @@ protected:
                       "finalize");
             dev.record_end(queue_);
             old_c_.swap(new_c_);
+            if (this->after_iteration(it, probe_, (uint32_t)d, (uint32_t)k, new_c_.data(), old_c_.data(), queue_))
+                break;
         }
         streamer_.finish();
         uint64_t total_time = total_timer.stop<std::chrono::nanoseconds>();
@@ -324,6 +329,7 @@ protected:
     ChunkStreamer<PointT, LabelT> streamer_;
     DeviceVector<PointT> old_c_, new_c_;
     DeviceVector<MassT> masses_;
+    ConvergenceProbe<PointT, LabelT, MassT> probe_;
     uint64_t last_total_ns_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
 };
 

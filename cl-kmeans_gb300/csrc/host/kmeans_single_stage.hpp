@@ -52,11 +52,15 @@ public:
 
         Timer::Timer total_timer;
         total_timer.start();
+        this->reset_progress();
         for (uint32_t iteration = 0; iteration < this->max_iterations; ++iteration) {
             engine_.launch(queue_, d, n, k, points_.data(), centroids_.data(), new_centroids_.data(),
                            labels_.data(), masses_.data(), CKM_MODE_FINALIZE,
                            this->measurement->add_datapoint((int)iteration), WaitList());
             centroids_.swap(new_centroids_);
+            if (this->after_iteration(iteration, probe_, (uint32_t)d, (uint32_t)k, new_centroids_.data(),
+                                      centroids_.data(), queue_))
+                break;
         }
         queue_.finish();
         uint64_t total_time = total_timer.stop<std::chrono::nanoseconds>();
@@ -102,6 +106,7 @@ private:
     }
 
     FusedLloyd<PointT, LabelT, MassT> engine_;
+    ConvergenceProbe<PointT, LabelT, MassT> probe_;
     Stream queue_;
     DeviceVector<PointT> points_, centroids_, new_centroids_;
     DeviceVector<LabelT> labels_;

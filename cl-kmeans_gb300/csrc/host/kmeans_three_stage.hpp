@@ -57,6 +57,8 @@ public:
         Timer::Timer total_timer;
         total_timer.start();
         Event cu_done;
+        this->reset_progress();
+        if (this->converge) prev_.resize(k * d);
         for (uint32_t it = 0; it < this->max_iterations; ++it) {
             WaitList ll_wait;
             ll_wait.insert(cu_done);
@@ -73,6 +75,10 @@ public:
             Event cu = cu_engine_.launch(q_centroid_update, d, n, k, points_.data(), centroids_.data(),
                                          labels_.data(), masses_.data(), CKM_MODE_DEFER,
                                          this->measurement->add_datapoint((int)it), cu_wait);
+            if (this->converge)  // the divide below overwrites the centroids in place
+                cuda_check(cudaMemcpyAsync(prev_.data(), centroids_.data(), k * d * sizeof(PointT),
+                                           cudaMemcpyDeviceToDevice, q_centroid_update.get()),
+                           "centroids copy");
             auto& dv = this->measurement->add_datapoint((int)it).set_name("MatrixBinaryOpRow");
             Event& dev = dv.add_event(q_centroid_update);
             ckm_check(Api<PointT, LabelT, MassT>::finalize((uint32_t)d, (uint32_t)k, centroids_.data(),
@@ -82,6 +88,9 @@ public:
             dev.record_end(q_centroid_update);
             cu_done = dev;
             (void)cu;
+            if (this->after_iteration(it, probe_, (uint32_t)d, (uint32_t)k, prev_.data(), centroids_.data(),
+                                      q_centroid_update))
+                break;
         }
         q_labeling.finish();
         q_mass_update.finish();
@@ -141,7 +150,8 @@ private:
 
     CentroidUpdate<PointT, LabelT, MassT> cu_engine_;
     Stream q_labeling, q_mass_update, q_centroid_update;
-    DeviceVector<PointT> points_, centroids_;
+    DeviceVector<PointT> points_, centroids_, prev_;
+    ConvergenceProbe<PointT, LabelT, MassT> probe_;
     DeviceVector<LabelT> labels_;
     DeviceVector<MassT> masses_;
     uint64_t last_total_ns_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;

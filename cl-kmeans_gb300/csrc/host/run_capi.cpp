@@ -45,12 +45,19 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
     try {
         if (cfg->device >= 0) cuda_check(cudaSetDevice(cfg->device), "cudaSetDevice");
         uint64_t total_ns = 0, h2d = 0, d2h = 0;
+        uint32_t done = 0, conv = 0;
+        float shift = 0.0f;
         if (pipeline == "single_stage") {
             KmeansSingleStage<P, L, M> s;
             FusedConfiguration fc;
             fc.strategy = or_default(cfg->fused_strategy, "feature_sum");
             s.set_fused(fc);
+            s.set_converge(cfg->converge != 0);
+            s.set_tolerance(cfg->tolerance);
             s.run_raw(iters, d, n, k, points, centroids, masses, labels);
+            done = (uint32_t)s.iterations_done();
+            conv = s.did_converge() ? 1u : 0u;
+            shift = s.last_shift();
             total_ns = s.last_total_ns();
             h2d = s.h2d_bytes();
             d2h = s.d2h_bytes();
@@ -65,7 +72,12 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
             s.set_labeler(lc);
             s.set_mass_updater(mc);
             s.set_centroid_updater(cc);
+            s.set_converge(cfg->converge != 0);
+            s.set_tolerance(cfg->tolerance);
             s.run_raw(iters, d, n, k, points, centroids, masses, labels);
+            done = (uint32_t)s.iterations_done();
+            conv = s.did_converge() ? 1u : 0u;
+            shift = s.last_shift();
             total_ns = s.last_total_ns();
             h2d = s.h2d_bytes();
             d2h = s.d2h_bytes();
@@ -79,7 +91,12 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
                 fc.strategy = or_default(cfg->fused_strategy, "feature_sum");
                 s.set_fused(fc);
                 s.set_options(opt);
+                s.set_converge(cfg->converge != 0);
+                s.set_tolerance(cfg->tolerance);
                 s.run_raw(iters, d, n, k, points, centroids, masses, labels);
+                done = (uint32_t)s.iterations_done();
+                conv = s.did_converge() ? 1u : 0u;
+                shift = s.last_shift();
                 total_ns = s.last_total_ns();
                 h2d = s.h2d_bytes();
                 d2h = s.d2h_bytes();
@@ -95,7 +112,12 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
                 s.set_mass_updater(mc);
                 s.set_centroid_updater(cc);
                 s.set_options(opt);
+                s.set_converge(cfg->converge != 0);
+                s.set_tolerance(cfg->tolerance);
                 s.run_raw(iters, d, n, k, points, centroids, masses, labels);
+                done = (uint32_t)s.iterations_done();
+                conv = s.did_converge() ? 1u : 0u;
+                shift = s.last_shift();
                 total_ns = s.last_total_ns();
                 h2d = s.h2d_bytes();
                 d2h = s.d2h_bytes();
@@ -108,7 +130,9 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
             info->h2d_bytes = h2d;
             info->d2h_bytes = d2h;
             info->kernel_launches = ckm::launch_count() - launches0;
-            info->iterations = iters;
+            info->iterations = done;
+            info->converged = conv;
+            info->last_shift = shift;
         }
         return CKM_OK;
     } catch (const KernelError& e) {

@@ -197,6 +197,15 @@ int ckm_centroid_update_f64(uint32_t num_features, uint64_t num_points, uint32_t
                             const uint64_t *masses, void *scratch, size_t scratch_bytes,
                             int mode, ckm_stream_t stream);
 
+/* Relative centroid shift of one iteration, written to the device float
+ * *shift: max |new - old| over max |old| (NaN entries, empty clusters, are
+ * skipped).  The convergence test of `kmeans.converge` (parsed but unused
+ * in the reference, configuration_parser.cpp:67, 143-145). */
+int ckm_centroid_shift_f32(uint32_t num_features, uint32_t num_clusters, const float *old_centroids,
+                           const float *new_centroids, float *shift, ckm_stream_t stream);
+int ckm_centroid_shift_f64(uint32_t num_features, uint32_t num_clusters, const double *old_centroids,
+                           const double *new_centroids, float *shift, ckm_stream_t stream);
+
 /* M[f*k + c] = M[f*k + c] / (PointT) masses[c].  Replaces
  * MatrixBinaryOp<PointT,MassT>::row with Divide
  * (cl_kernels/matrix_binary_op.hpp:86-127; matrix_binary_op.cl:98-114). */
@@ -323,6 +332,9 @@ typedef struct ckm_run_config {
     int device;                            /* CUDA device ordinal */
     uint64_t device_budget_bytes;          /* buffered pipelines: device-memory cap (0 = auto) */
     uint64_t chunk_bytes;                  /* buffered pipelines: points bytes per chunk (0 = auto) */
+    int converge;                          /* kmeans.converge: stop once the relative centroid shift
+                                              (ckm_centroid_shift_*) falls below tolerance */
+    double tolerance;                      /* 0 = 1e-4 */
 } ckm_run_config;
 
 typedef struct ckm_run_info {
@@ -331,6 +343,8 @@ typedef struct ckm_run_info {
     uint64_t d2h_bytes;          /* device -> host bytes moved by the call */
     uint64_t kernel_launches;    /* kernels this library launched */
     uint32_t iterations;         /* iterations run */
+    uint32_t converged;          /* 1 if the run stopped on the convergence test */
+    float last_shift;            /* relative centroid shift of the last iteration (converge runs; else 0) */
 } ckm_run_info;
 
 /* centroids: in = initial, out = final (k = num_clusters).  masses, labels:

@@ -133,3 +133,17 @@ def test_binary_header(ckm, tmp_path):
     assert info == {"num_features": "7", "num_clusters": "0", "num_points": "1234"}
     r = subprocess.run([bench_bin(ckm), "--info", str(tmp_path / "missing.bin")], capture_output=True, text=True)
     assert r.returncode != 0 and "cannot open" in r.stderr
+
+
+def test_converge_and_tolerance_keys(ckm, tmp_path):
+    """kmeans.converge (parsed but unused in the reference,
+    configuration_parser.cpp:67, 143-145) drives the convergence test here;
+    its tolerance is [kmeans.gb300] tolerance, a positive real (default 1e-4)."""
+    base = "[kmeans]\nclusters = 4\npipeline = single_stage\niterations = 50\nconverge = true\n"
+    c = parse(ckm, tmp_path, base)
+    assert c["kmeans.converge"] == "1" and float(c["kmeans.gb300.tolerance"]) == 1e-4
+    c = parse(ckm, tmp_path, base + "[kmeans.gb300]\ntolerance = 2.5e-3\n")
+    assert float(c["kmeans.gb300.tolerance"]) == 2.5e-3
+    for bad in ("0", "-1e-3", "abc"):
+        with pytest.raises(ValueError):
+            parse(ckm, tmp_path, base + "[kmeans.gb300]\ntolerance = %s\n" % bad)

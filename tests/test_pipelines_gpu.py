@@ -186,3 +186,46 @@ def test_generator_ex_laws(ckm, cuda):
     assert np.isfinite(x).all()
     assert 1.0 < x.std() < 4.0          # N(0, 4) centres plus sigma <= 1
     assert abs(x.mean()) < 1.0
+
+
+@pytest.mark.parametrize("pipeline", ["single_stage", "three_stage", "single_stage_buffered",
+                                      "three_stage_buffered"])
+def test_convergence_stops_early(ckm, oracle, cuda, pipeline):
+    """kmeans.converge: the run stops after the first iteration whose relative
+    centroid shift is below the tolerance, with the same result as a fixed run
+    of that many iterations."""
+    n, d, k = 60000, 3, 6
+    P = blobs(n, d, k, seed=5, spread=8.0, sigma=0.6)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    extra = {}
+    if pipeline.endswith("buffered"):
+        extra = dict(chunk_bytes=16000 * d * 4, device_budget_bytes=(16000 * (d + 1) * 4) * 5 + (1 << 20) + 65536)
+    C, M, L, info = ckm.kmeans_run(P, d, k, 200, C0, pipeline=pipeline, converge=True, tolerance=1e-5, **extra)
+    assert info.converged == 1 and 2 <= info.iterations < 200
+    assert 0.0 <= info.last_shift < 1e-5
+    C2, M2, L2, info2 = ckm.kmeans_run(P, d, k, info.iterations, C0, pipeline=pipeline, **extra)
+    assert info2.converged == 0 and info2.iterations == info.iterations
+    assert np.array_equal(L, L2) and np.array_equal(M, M2)
+    assert np.allclose(C, C2, rtol=1e-6, atol=1e-6 * np.abs(P).max())
+    _e2e_check(oracle, P, n, d, k, info.iterations, C0, C, M, L)
+
+
+def test_centroid_shift_matches_numpy(ckm, cuda):
+    """ckm_centroid_shift_*: max |new - old| / max |old|, NaN entries skipped."""
+    import ctypes
+    import torch
+    rng = np.random.default_rng(9)
+    d, k = 7, 33
+    old = rng.normal(size=k * d).astype(np.float32)
+    new = (old + rng.normal(scale=1e-3, size=k * d)).astype(np.float32)
+    new[5] = np.nan  # an empty cluster's coordinate
+    want = np.nanmax(np.abs(new.astype(np.float64) - old)) / np.abs(old).max()
+    dO, dN = to_dev(old, cuda), to_dev(new, cuda)
+    out = torch.zeros(1, dtype=torch.float32, device=cuda)
+    L = ckm.lib()
+    L.ckm_centroid_shift_f32.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p]
+    s = torch.cuda.current_stream()
+    assert L.ckm_centroid_shift_f32(d, k, dO.data_ptr(), dN.data_ptr(), out.data_ptr(), s.cuda_stream) == 0
+    torch.cuda.synchronize()
+    assert abs(float(out.item()) - want) <= 1e-6 * want
