@@ -537,6 +537,10 @@ def main():
                "h2d_bytes_per_step": int(info.h2d_bytes), "d2h_bytes_per_step": int(info.d2h_bytes),
                "iterations_per_step": iters_cfg, "ms_per_step": e2e_t * 1e3,
                "total_time_window_ms": info.total_time_ns / 1e6}
+        # the link that bounds the copies inside e2e: pinned H2D, 64 MiB chunks
+        link_best, _ = ckm.transfer_probe(64 << 20, repeat=16, pinned=True, to_device=True, device=local)
+        e2e["h2d_link_gbs"] = link_best
+        e2e["h2d_link_ms_per_step"] = info.h2d_bytes / (link_best * 1e9) * 1e3 if link_best > 0 else None
         del hostP
 
     # --- CPU baseline (oracle port, single thread, bounded sample) ---------

@@ -465,7 +465,21 @@ class MixtureSpec(ctypes.Structure):
 
 
 EXPORTS.append("ckm_generate_mixture_ex_f32")
-EXPORTS += ["ckm_centroid_shift_f32", "ckm_centroid_shift_f64"]
+EXPORTS += ["ckm_centroid_shift_f32", "ckm_centroid_shift_f64", "ckm_transfer_probe"]
+
+
+def transfer_probe(chunk_bytes, repeat=10, pinned=True, to_device=True, trials=3, device=0):
+    """ckm_transfer_probe: (best, mean) GB/s of `repeat` back-to-back copies
+    of chunk_bytes between host memory and the device."""
+    L = lib()
+    fn = L.ckm_transfer_probe
+    fn.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
+                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    fn.restype = ctypes.c_int
+    best, mean = ctypes.c_double(), ctypes.c_double()
+    check(fn(device, chunk_bytes, repeat, 1 if pinned else 0, 1 if to_device else 0, trials, ctypes.byref(best),
+             ctypes.byref(mean)), "ckm_transfer_probe")
+    return best.value, mean.value
 
 
 def generate_mixture_ex(points, n, d, blobs, seed, center=("uniform", -10.0, 10.0), sigma=("uniform", 1.0, 1.0),

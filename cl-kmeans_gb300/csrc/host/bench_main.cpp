@@ -95,6 +95,14 @@ public:
                 sigma_lo_ = std::stof(take("--sigma-lo"));
             } else if (key == "--sigma-hi") {
                 sigma_hi_ = std::stof(take("--sigma-hi"));
+            } else if (key == "--transfer") {
+                transfer_ = true;
+            } else if (key == "--max-size") {
+                max_size_mib_ = std::stoull(take("--max-size"));
+            } else if (key == "--repeat") {
+                repeat_ = (uint32_t)std::stoul(take("--repeat"));
+            } else if (key == "--device") {
+                device_ = std::stoi(take("--device"));
             } else if (!a.empty() && a[0] == '-') {
                 throw std::invalid_argument("unrecognised option '" + a + "'");
             } else {
@@ -114,10 +122,12 @@ public:
                          "  --generate OUT        Write a seeded mixture file (--points --features --blobs\n"
                          "                        --seed --sigma-lo --sigma-hi)\n"
                          "  --print-config        Print the parsed configuration (one key=value per line)\n"
-                         "  --info                Print the header of the input file\n";
+                         "  --info                Print the header of the input file\n"
+                         "  --transfer            Host<->device link probe (--max-size MiB, default 256;\n"
+                         "                        --repeat copies per size, default 10; --device)\n";
             return -1;
         }
-        if (!generate_.empty()) return 1;
+        if (!generate_.empty() || transfer_) return 1;
         if (info_) {
             if (input_file_.empty()) {
                 std::cout << "No input file specified." << std::endl;
@@ -149,7 +159,33 @@ public:
     uint64_t gen_points_ = 1 << 20, gen_seed_ = 42;
     uint32_t gen_features_ = 4, gen_blobs_ = 10;
     float sigma_lo_ = 1.0f, sigma_hi_ = 1.0f;
+    bool transfer_ = false;
+    uint64_t max_size_mib_ = 256;
+    uint32_t repeat_ = 10;
+    int device_ = 0;
 };
+
+// --transfer: the link probe for chunk sizes 1 MiB .. --max-size MiB
+// (doubling), both directions, pinned and pageable host memory.
+int transfer_bench(const CmdOptions& o) {
+    std::cout << "direction,host_memory,chunk_mib,repeat,best_gbs,mean_gbs" << std::endl;
+    for (uint64_t mib = 1; mib <= std::max<uint64_t>(o.max_size_mib_, 1); mib *= 2) {
+        for (int to_device = 1; to_device >= 0; --to_device) {
+            for (int pinned = 1; pinned >= 0; --pinned) {
+                double best = 0.0, mean = 0.0;
+                const int rc = ckm_transfer_probe(o.device_, mib << 20, std::max<uint32_t>(o.repeat_, 1), pinned,
+                                                  to_device, 3, &best, &mean);
+                if (rc != CKM_OK) {
+                    std::cerr << "ckm_bench: transfer probe failed: " << ckm_last_error() << std::endl;
+                    return -1;
+                }
+                std::printf("%s,%s,%llu,%u,%.2f,%.2f\n", to_device ? "H2D" : "D2H", pinned ? "pinned" : "pageable",
+                            (unsigned long long)mib, std::max<uint32_t>(o.repeat_, 1), best, mean);
+            }
+        }
+    }
+    return 1;
+}
 
 // Verification reference: the arithmetic of the reference's KmeansNaive
 // (kmeans_naive.cpp:40-103): fma distance, strict '<' argmin, Kahan sums.
@@ -472,6 +508,7 @@ int main(int argc, char** argv) {
         CmdOptions options;
         if (options.parse(argc, argv) < 0) return options.help_ ? 0 : 1;
         if (!options.generate_.empty()) return generate(options) > 0 ? 0 : 1;
+        if (options.transfer_) return transfer_bench(options) > 0 ? 0 : 1;
         if (options.info_) return file_info(options.input_file_) > 0 ? 0 : 1;
         ConfigurationParser config;
         config.parse_file(options.config_file_);

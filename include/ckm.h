@@ -358,6 +358,18 @@ int ckm_kmeans_run_f64(const ckm_run_config *config, uint32_t max_iterations,
                        const double *host_points, double *host_centroids, uint64_t *host_masses,
                        uint64_t *host_labels, ckm_run_info *info);
 
+/* Host <-> device link probe (the roofline of the buffered pipelines, whose
+ * points cross this link every iteration).  Times `repeat` back-to-back
+ * copies of chunk_bytes between host memory (pinned != 0: page-locked,
+ * else pageable) and one device buffer, to the device (to_device != 0) or
+ * back, over `trials` timed trials after one warm-up; reports the best and
+ * mean GB/s (mean_gbs may be NULL).  device < 0 keeps the current device.
+ * It allocates its own host and device buffers.  Replaces the measurement of
+ * transfer_bench.cpp (buffer sizes up to --max-size pushed through the
+ * buffer cache, --repeat times). */
+int ckm_transfer_probe(int device, uint64_t chunk_bytes, uint32_t repeat, int pinned, int to_device,
+                       uint32_t trials, double *best_gbs, double *mean_gbs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,3 +122,28 @@ def test_generate_then_read(ckm, cuda, tmp_path):
     assert list(hdr) == [5, 0, 10000]
     body = np.fromfile(f, np.float32, offset=24)
     assert body.size == 50000 and np.isfinite(body).all()
+
+
+def test_transfer_probe(ckm, cuda):
+    """ckm_transfer_probe: positive, plausible link throughputs in both
+    directions for pinned and pageable host memory."""
+    best, mean = ckm.transfer_probe(16 << 20, repeat=8, pinned=True, to_device=True)
+    assert 1.0 < best < 2000.0 and 0.0 < mean <= best * (1 + 1e-9)
+    for pinned, to_device in ((True, False), (False, True), (False, False)):
+        b, m = ckm.transfer_probe(4 << 20, repeat=4, pinned=pinned, to_device=to_device)
+        assert b > 0.0 and m > 0.0
+
+
+def test_bench_transfer_mode(ckm, cuda):
+    """ckm_bench --transfer (the reference's transfer_bench measurement):
+    one CSV line per chunk size, direction and host memory kind."""
+    import subprocess
+    r = subprocess.run([ckm.BENCH_BIN, "--transfer", "--max-size", "4", "--repeat", "4"], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert lines[0] == "direction,host_memory,chunk_mib,repeat,best_gbs,mean_gbs"
+    rows = [l.split(",") for l in lines[1:]]
+    assert len(rows) == 3 * 4   # 1, 2, 4 MiB x {H2D, D2H} x {pinned, pageable}
+    assert {r[0] for r in rows} == {"H2D", "D2H"} and {r[1] for r in rows} == {"pinned", "pageable"}
+    assert all(float(r[4]) > 0 for r in rows)
