@@ -287,6 +287,30 @@ def run_batched_workload(args, ckm, torch, dev):
         if ok.any():
             scale = max(float(np.abs(b[ok]).max()), 1e-30)
             worst = max(worst, float(np.abs(a[ok] - b[ok]).max()) / scale)
+    diverged = 0
+    for j, ref in zip(jobs, plain_result):
+        a, b = j["centroids"].cpu().numpy(), ref.cpu().numpy()
+        ok = ~(np.isnan(a) | np.isnan(b))
+        if ok.any() and np.abs(a[ok] - b[ok]).max() > 1e-5 * max(float(np.abs(b[ok]).max()), 1e-30):
+            diverged += 1
+    # lockstep: one iteration of every job from the same centroids, batched
+    # against the plain fused call (the per-iteration agreement; after 20
+    # iterations a near-tie flip can send a job down another trajectory)
+    for j in jobs:
+        j["centroids"].copy_(j["init"])
+    batch.run(1, use_graph=False)
+    lock_worst, lock_label_diff = 0.0, 0
+    for j, a in zip(jobs, alt):
+        key = (j["d"], j["k"])
+        lab = torch.empty_like(j["labels"])
+        mas = torch.empty_like(j["masses"])
+        ckm.fused(j["points"], j["init"], a, lab, mas, scratch[key], j["n"], j["d"], j["k"], ckm.MODE_FINALIZE, stream)
+        torch.cuda.synchronize()
+        lock_label_diff += int((lab != j["labels"]).sum().item())
+        x, y = j["centroids"].cpu().numpy(), a.cpu().numpy()
+        ok = ~(np.isnan(x) | np.isnan(y))
+        if ok.any():
+            lock_worst = max(lock_worst, float(np.abs(x[ok] - y[ok]).max()) / max(float(np.abs(y[ok]).max()), 1e-30))
     batch.close()
     line = {
         "metric": "jobs/s", "value": num_jobs / batch_s, "unit": "jobs/s", "n_gpus": 1, "steps": len(times),
@@ -298,7 +322,8 @@ def run_batched_workload(args, ckm, torch, dev):
                                "launches": num_jobs * iters},
         "speedup_vs_plain_loop": plain_s / batch_s,
         "pts_iter_per_s": total_pts * iters / batch_s,
-        "max_rel_centroid_diff_vs_plain_loop": worst,
+        "lockstep_vs_plain": {"max_rel_centroid_diff": lock_worst, "label_mismatches": lock_label_diff},
+        "after_20_iterations_vs_plain": {"max_rel_centroid_diff": worst, "jobs_beyond_1e-5": diverged},
         "gpu_launches": int(gpu_launches),
     }
     print(json.dumps(line), flush=True)

@@ -1,10 +1,10 @@
 // Host side of the batched Lloyd iteration: the ckm_batch handle.
 //
 // create: uploads a device job table, allocates every job's FP64 scratch and
-//         second centroid buffer in two arenas, and builds the CTA schedule:
-//         the jobs' tiles laid end to end, cut into `grid` runs of equal
-//         estimated cost (points x (k*d + 2*(d+1) + 16)), each run split at
-//         job boundaries into segments.  With autotune, candidate (tile size,
+//         second centroid buffer in two arenas, and builds the work list:
+//         every job's tiles cut into segments of similar estimated cost
+//         (see build_schedule), largest first, claimed by the CTAs at run
+//         time.  With autotune, candidate (tile size,
 //         CTAs per SM) pairs are timed on the batch itself (two steps each,
 //         with the device job state saved and restored around them).
 // step:   one persistent kernel launch.
@@ -36,7 +36,7 @@ struct ckm_batch {
     unsigned char* d_scratch = nullptr;   // per job: sums (8 k d) + msum (8 k), 256-aligned
     float* d_alt = nullptr;               // per job: second centroid buffer (4 k d)
     BatchSegment* d_segs = nullptr;
-    uint32_t* d_seg_off = nullptr;
+    unsigned int* d_work = nullptr;        // segments claimed in the current step
     // schedule
     uint32_t grid = 0, tile = 1024, ctas_per_sm = 1, flush = 16, segments = 0;
     size_t cent_cap = 0, acc_cap = 0;
@@ -55,42 +55,40 @@ int cuda_alloc(void** p, size_t bytes, const char* what) {
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, what);
 }
 
-// Builds the segment list for (tile, grid) into host vectors.
+// Builds the work list for (tile, grid): every job's tiles cut into segments
+// of about 1/8 of a CTA's share of the estimated cost, largest first.  Cost
+// per point: the distances (k*d) plus the shared-memory adds of the sums,
+// which contend more the fewer clusters there are (d * (1 + 32/k) * 4), plus
+// a constant.
 void build_schedule(const std::vector<ckm_batch_job>& jobs, uint32_t tile, uint32_t grid,
-                    std::vector<BatchSegment>& segs, std::vector<uint32_t>& off, std::vector<uint32_t>& tiles_per_job) {
+                    std::vector<BatchSegment>& segs, std::vector<uint32_t>& tiles_per_job) {
     const uint32_t J = (uint32_t)jobs.size();
     tiles_per_job.assign(J, 0);
     double total = 0.0;
     std::vector<double> tile_cost(J, 0.0);
     for (uint32_t j = 0; j < J; ++j) {
         const ckm_batch_job& b = jobs[j];
+        const double k = (double)b.num_clusters, d = (double)b.num_features;
         tiles_per_job[j] = (uint32_t)((b.num_points + tile - 1) / tile);
-        tile_cost[j] = (double)tile * ((double)b.num_clusters * b.num_features + 2.0 * (b.num_features + 1) + 16.0);
+        tile_cost[j] = (double)tile * (k * d + 4.0 * d * (1.0 + 32.0 / k) + 32.0);
         total += tile_cost[j] * tiles_per_job[j];
     }
-    const double target = total / std::max<uint32_t>(grid, 1);
-    segs.clear();
-    off.assign(grid + 1, 0);
-    uint32_t cta = 0;
-    double acc = 0.0;
+    const double unit = total / (8.0 * std::max<uint32_t>(grid, 1));
+    std::vector<std::pair<double, BatchSegment>> units;
     for (uint32_t j = 0; j < J; ++j) {
-        uint32_t t = 0;
-        while (t < tiles_per_job[j]) {
-            // tiles this CTA can still take within its cost share
-            double room = target * (cta + 1) - acc;
-            uint32_t take = (cta + 1 >= grid) ? tiles_per_job[j] - t
-                                              : (uint32_t)std::max(1.0, std::floor(room / tile_cost[j] + 0.5));
-            take = std::min(take, tiles_per_job[j] - t);
-            segs.push_back(BatchSegment{j, t, t + take, 0});
-            acc += take * tile_cost[j];
-            t += take;
-            if (cta + 1 < grid && acc >= target * (cta + 1) - 0.5 * tile_cost[j]) {
-                off[cta + 1] = (uint32_t)segs.size();
-                ++cta;
-            }
+        const uint32_t per = (uint32_t)std::max(1.0, std::floor(unit / std::max(tile_cost[j], 1.0)));
+        for (uint32_t t = 0; t < tiles_per_job[j]; t += per) {
+            const uint32_t te = std::min(tiles_per_job[j], t + per);
+            units.push_back({tile_cost[j] * (te - t), BatchSegment{j, t, te, 0}});
         }
     }
-    for (uint32_t c = cta + 1; c <= grid; ++c) off[c] = (uint32_t)segs.size();
+    std::stable_sort(units.begin(), units.end(),
+                     [](const std::pair<double, BatchSegment>& a, const std::pair<double, BatchSegment>& b) {
+                         return a.first > b.first;
+                     });
+    segs.clear();
+    segs.reserve(units.size());
+    for (const auto& u : units) segs.push_back(u.second);
 }
 
 int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStream_t s) {
@@ -112,20 +110,16 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
     const uint32_t cps = std::min<uint32_t>(ctas_per_sm, (uint32_t)bps);
     const uint32_t grid = (uint32_t)di.sm_count * cps;
     std::vector<BatchSegment> segs;
-    std::vector<uint32_t> off, tiles;
-    build_schedule(b->jobs, tile, grid, segs, off, tiles);
+    std::vector<uint32_t> tiles;
+    build_schedule(b->jobs, tile, grid, segs, tiles);
     if (segs.size() > b->seg_capacity) {
         if (b->d_segs) cudaFree(b->d_segs);
         b->d_segs = nullptr;
         b->seg_capacity = segs.size() + 64;
         if ((st = cuda_alloc((void**)&b->d_segs, b->seg_capacity * sizeof(BatchSegment), "cudaMalloc(segments)"))) return st;
     }
-    if (b->d_seg_off) cudaFree(b->d_seg_off);
-    b->d_seg_off = nullptr;
-    if ((st = cuda_alloc((void**)&b->d_seg_off, off.size() * sizeof(uint32_t), "cudaMalloc(segment offsets)"))) return st;
+    if (!b->d_work && (st = cuda_alloc((void**)&b->d_work, sizeof(unsigned int), "cudaMalloc(work counter)"))) return st;
     cudaError_t e = cudaMemcpyAsync(b->d_segs, segs.data(), segs.size() * sizeof(BatchSegment), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->d_seg_off, off.data(), off.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
     for (uint32_t j = 0; j < b->num_jobs; ++j) b->host_dev_jobs[j].num_tiles = tiles[j];
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b->d_jobs, b->host_dev_jobs.data(), b->num_jobs * sizeof(BatchJobDev), cudaMemcpyHostToDevice, s);
@@ -143,7 +137,8 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
 }
 
 int step(ckm_batch* b, cudaStream_t s) {
-    return launch_batched(b->d_jobs, b->d_segs, b->d_seg_off, b->grid, b->tile, b->flush, b->cent_cap, b->acc_cap, s);
+    return launch_batched(b->d_jobs, b->d_segs, b->segments, b->d_work, b->grid, b->tile, b->flush, b->cent_cap,
+                          b->acc_cap, s);
 }
 
 int autotune(ckm_batch* b, cudaStream_t s) {
@@ -204,7 +199,7 @@ void release(ckm_batch* b) {
     cudaFree(b->d_scratch);
     cudaFree(b->d_alt);
     cudaFree(b->d_segs);
-    cudaFree(b->d_seg_off);
+    cudaFree(b->d_work);
 }
 
 }  // namespace

@@ -1,10 +1,13 @@
 // Batched Lloyd iterations: many independent k-means jobs of uneven n, d and
 // k in ONE persistent launch per iteration.
 //
-// The host cuts every job into tiles of `tile` points and assigns contiguous
-// runs of tiles ("segments", never spanning two jobs) to the CTAs so that the
-// estimated cost (points x (k*d + overhead)) per CTA is balanced.  A CTA walks
-// its segments; per segment it stages the job's centroids in shared memory,
+// The host cuts every job into tiles of `tile` points and groups contiguous
+// runs of tiles ("segments", never spanning two jobs) into units of similar
+// estimated cost, listed largest first.  The CTAs claim segments from a
+// counter until none are left (dynamic scheduling: a static split by
+// estimated cost left most SMs idle behind a few slow CTAs, because small-k
+// jobs pay for shared-memory atomic contention that the estimate does not
+// see).  Per segment a CTA stages the job's centroids in shared memory,
 // labels each point with the reference's exact arithmetic (fma(t,t,acc) over
 // the features, strict '<' argmin from cluster 0; kmeans_naive.cpp:48-63) and
 // adds it into a shared-memory sum/mass table, which it merges into the job's
@@ -190,13 +193,18 @@ __device__ void finalize_job(const BatchJobDev& J, int parity) {
 }
 
 __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restrict__ jobs,
-                                                     const BatchSegment* __restrict__ segs,
-                                                     const uint32_t* __restrict__ seg_off, uint32_t tile,
+                                                     const BatchSegment* __restrict__ segs, uint32_t num_segs,
+                                                     unsigned int* __restrict__ work, uint32_t tile,
                                                      uint32_t flush_tiles, size_t cent_cap, size_t acc_cap) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned int s_last;
-    const uint32_t s0 = seg_off[blockIdx.x], s1 = seg_off[blockIdx.x + 1];
-    for (uint32_t si = s0; si < s1; ++si) {
+    __shared__ unsigned int s_last, s_unit;
+    for (;;) {
+        // dynamic schedule: the next unclaimed segment (largest first)
+        __syncthreads();  // every thread has read the previous s_unit
+        if (threadIdx.x == 0) s_unit = atomicAdd(work, 1u);
+        __syncthreads();
+        const uint32_t si = s_unit;
+        if (si >= num_segs) break;
         const BatchSegment S = segs[si];
         const BatchJobDev J = jobs[S.job];
         // parity and flags were last written by the previous launch (or by the
@@ -277,13 +285,15 @@ int ensure_batched_attr() {
 
 }  // namespace
 
-int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, const uint32_t* seg_off, uint32_t grid,
-                   uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s) {
+int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
+                   uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s) {
     const size_t smem = cent_cap + acc_cap;
     int st = ensure_batched_attr();
     if (st) return st;
     if (grid == 0) return CKM_OK;
-    batched_kernel<<<grid, BT, smem, s>>>(jobs, segs, seg_off, tile, flush_tiles, cent_cap, acc_cap);
+    cudaError_t e0 = cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
+    if (e0 != cudaSuccess) return cuda_fail(e0, "batched work counter");
+    batched_kernel<<<grid, BT, smem, s>>>(jobs, segs, num_segs, work, tile, flush_tiles, cent_cap, acc_cap);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batched launch");

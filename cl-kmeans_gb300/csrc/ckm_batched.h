@@ -30,13 +30,15 @@ struct BatchJobDev {
     uint32_t pad;
 };
 
-// A contiguous run of one job's tiles processed by one CTA.
+// A contiguous run of one job's tiles: one unit of work, claimed by a CTA.
 struct BatchSegment {
     uint32_t job, tile_begin, tile_end, pad;
 };
 
-int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, const uint32_t* seg_off, uint32_t grid,
-                   uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s);
+// One step: the CTAs claim segments in list order (largest first) from the
+// counter *work, which the launch resets to zero beforehand.
+int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
+                   uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s);
 int batched_blocks_per_sm(size_t smem, int* out);
 // Copies cent[1] into cent[0] for every job whose parity is 1 and resets the
 // parity, so the caller's centroid arrays hold the current centroids.
