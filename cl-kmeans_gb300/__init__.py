@@ -286,6 +286,8 @@ class BatchOptions(ctypes.Structure):
         ("ctas_per_sm", ctypes.c_uint32),
         ("flush_tiles", ctypes.c_uint32),
         ("autotune", ctypes.c_int),
+        ("tolerance", ctypes.c_float),
+        ("max_iterations", ctypes.c_uint32),
     ]
 
 
@@ -318,14 +320,15 @@ class Batch:
     """Owns a ckm_batch handle over torch device tensors (per job: points,
     centroids, labels, masses).  The tensors must outlive the batch."""
 
-    def __init__(self, jobs, tile_points=0, ctas_per_sm=0, flush_tiles=0, autotune=False, stream=None):
+    def __init__(self, jobs, tile_points=0, ctas_per_sm=0, flush_tiles=0, autotune=False, stream=None,
+                 tolerance=0.0, max_iterations=0):
         L = _batch_lib()
         self._keep = jobs
         arr = (BatchJob * len(jobs))()
         for i, j in enumerate(jobs):
             arr[i] = BatchJob(j["points"].data_ptr(), j["centroids"].data_ptr(), j["labels"].data_ptr(),
                               j["masses"].data_ptr(), j["n"], j["d"], j["k"])
-        opt = BatchOptions(tile_points, ctas_per_sm, flush_tiles, 1 if autotune else 0)
+        opt = BatchOptions(tile_points, ctas_per_sm, flush_tiles, 1 if autotune else 0, tolerance, max_iterations)
         h = ctypes.c_void_p()
         check(L.ckm_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(jobs), ctypes.byref(opt), ctypes.byref(h),
                                  _stream(stream)), "ckm_batch_create")

@@ -39,6 +39,9 @@ struct ckm_batch {
     unsigned int* d_work = nullptr;        // segments claimed in the current step
     // schedule
     uint32_t grid = 0, tile = 1024, ctas_per_sm = 1, flush = 16, segments = 0;
+    float tol = 0.f;                      // convergence stop (0: none)
+    uint32_t max_it = 0;                  // iteration cap (0: none)
+    uint32_t jobs_capacity = 0;           // entries of d_jobs
     size_t cent_cap = 0, acc_cap = 0;
     std::vector<BatchJobDev> host_dev_jobs;
     // graphs per iteration count
@@ -137,8 +140,8 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
 }
 
 int step(ckm_batch* b, cudaStream_t s) {
-    return launch_batched(b->d_jobs, b->d_segs, b->segments, b->d_work, b->grid, b->tile, b->flush, b->cent_cap,
-                          b->acc_cap, s);
+    return launch_batched(b->d_jobs, b->d_segs, b->segments, b->d_work, b->tol, b->max_it, b->grid, b->tile, b->flush,
+                          b->cent_cap, b->acc_cap, s);
 }
 
 int autotune(ckm_batch* b, cudaStream_t s) {
@@ -230,6 +233,9 @@ int ckm_batch_create(const ckm_batch_job* jobs, uint32_t num_jobs, const ckm_bat
     ckm_batch_options opt{};
     if (options) opt = *options;
     b->flush = opt.flush_tiles ? opt.flush_tiles : 16;
+    b->tol = opt.tolerance > 0.f ? opt.tolerance : 0.f;
+    b->max_it = opt.max_iterations;
+    b->jobs_capacity = num_jobs;
     // arenas
     size_t scratch_total = 0, alt_total = 0;
     std::vector<size_t> s_off(num_jobs), a_off(num_jobs);
@@ -392,3 +398,52 @@ int ckm_batch_destroy(ckm_batch* b) {
 }
 
 }  // extern "C"
+
+namespace ckm {
+
+int batch_create_external(::ckm_batch** out) {
+    if (!out) return fail(CKM_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = new ckm_batch();
+    cudaGetDevice(&(*out)->device);
+    return CKM_OK;
+}
+
+int batch_set_jobs(::ckm_batch* b, const BatchJobDev* jobs, uint32_t num_jobs, uint32_t tile, uint32_t ctas_per_sm,
+                   float tol, uint32_t max_it, cudaStream_t s) {
+    if (!b || (num_jobs && !jobs)) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (num_jobs > b->jobs_capacity) {
+        cudaFree(b->d_jobs);
+        b->d_jobs = nullptr;
+        b->jobs_capacity = num_jobs + 256;
+        int st = cuda_alloc((void**)&b->d_jobs, b->jobs_capacity * sizeof(BatchJobDev), "cudaMalloc(job table)");
+        if (st) {
+            b->jobs_capacity = 0;
+            return st;
+        }
+    }
+    b->num_jobs = num_jobs;
+    b->host_dev_jobs.assign(jobs, jobs + num_jobs);
+    b->jobs.resize(num_jobs);
+    for (uint32_t j = 0; j < num_jobs; ++j) {
+        ckm_batch_job& u = b->jobs[j];
+        std::memset(&u, 0, sizeof(u));
+        u.num_points = jobs[j].n;
+        u.num_features = jobs[j].d;
+        u.num_clusters = jobs[j].k;
+    }
+    b->tol = tol;
+    b->max_it = max_it;
+    if (num_jobs == 0) {
+        b->segments = 0;
+        return CKM_OK;
+    }
+    return upload_schedule(b, tile, ctas_per_sm, s);
+}
+
+int batch_launch_step(::ckm_batch* b, cudaStream_t s) {
+    if (!b) return fail(CKM_ERR_INVALID_ARGUMENT, "batch is NULL");
+    if (b->num_jobs == 0 || b->segments == 0) return CKM_OK;
+    return step(b, s);
+}
+
+}  // namespace ckm

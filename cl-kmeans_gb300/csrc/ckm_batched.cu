@@ -148,7 +148,7 @@ __device__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s
 }
 
 // Last CTA of a job: centroids, masses, relative shift; scratch back to zero.
-__device__ void finalize_job(const BatchJobDev& J, int parity) {
+__device__ void finalize_job(const BatchJobDev& J, int parity, float tol, uint32_t max_it) {
     __shared__ float s_red[BT / 32 * 2];
     const uint32_t k = J.k, d = J.d;
     const float* old = J.cent[parity];
@@ -185,8 +185,14 @@ __device__ void finalize_job(const BatchJobDev& J, int parity) {
             a = fmaxf(a, s_red[w]);
             b = fmaxf(b, s_red[BT / 32 + w]);
         }
-        J.status->shift = a / fmaxf(b, 1e-30f);
-        J.status->iterations += 1;
+        const float shift = a / fmaxf(b, 1e-30f);
+        const uint32_t its = J.status->iterations + 1;
+        J.status->shift = shift;
+        J.status->iterations = its;
+        // convergence stop: the job parks itself (bit 0: skipped by later
+        // steps; bit 1: finished) once its shift is below the tolerance or it
+        // has run max_it iterations
+        if ((tol > 0.f && shift < tol) || (max_it != 0u && its >= max_it)) J.status->flags |= 3u;
         J.status->parity = (uint32_t)(parity ^ 1);
         *J.ticket = 0u;
     }
@@ -194,7 +200,8 @@ __device__ void finalize_job(const BatchJobDev& J, int parity) {
 
 __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restrict__ jobs,
                                                      const BatchSegment* __restrict__ segs, uint32_t num_segs,
-                                                     unsigned int* __restrict__ work, uint32_t tile,
+                                                     unsigned int* __restrict__ work, float tol, uint32_t max_it,
+                                                     uint32_t tile,
                                                      uint32_t flush_tiles, size_t cent_cap, size_t acc_cap) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned int s_last, s_unit;
@@ -260,7 +267,7 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
         __syncthreads();
         if (s_last) {
             __threadfence();
-            finalize_job(J, parity);
+            finalize_job(J, parity, tol, max_it);
         }
     }
 }
@@ -286,14 +293,16 @@ int ensure_batched_attr() {
 }  // namespace
 
 int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
-                   uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s) {
+                   float tol, uint32_t max_it, uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap,
+                   size_t acc_cap, cudaStream_t s) {
     const size_t smem = cent_cap + acc_cap;
     int st = ensure_batched_attr();
     if (st) return st;
     if (grid == 0) return CKM_OK;
     cudaError_t e0 = cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
     if (e0 != cudaSuccess) return cuda_fail(e0, "batched work counter");
-    batched_kernel<<<grid, BT, smem, s>>>(jobs, segs, num_segs, work, tile, flush_tiles, cent_cap, acc_cap);
+    batched_kernel<<<grid, BT, smem, s>>>(jobs, segs, num_segs, work, tol, max_it, tile, flush_tiles, cent_cap,
+                                          acc_cap);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batched launch");

@@ -5,6 +5,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+struct ckm_batch;  // include/ckm.h
+
 namespace ckm {
 
 // Per-job state kept on the device between iterations.
@@ -12,7 +14,7 @@ struct BatchStatus {
     float shift;          // max |new - old| / max |old| of the last iteration
     uint32_t iterations;  // iterations finished
     uint32_t parity;      // centroids live in cent[parity]; flipped by the finalising CTA
-    uint32_t flags;       // bit 0: inactive (skipped by the step)
+    uint32_t flags;       // bit 0: inactive (skipped by the step); bit 1: finished (converged or max iterations)
 };
 
 struct BatchJobDev {
@@ -36,12 +38,24 @@ struct BatchSegment {
 };
 
 // One step: the CTAs claim segments in list order (largest first) from the
-// counter *work, which the launch resets to zero beforehand.
+// counter *work, which the launch resets to zero beforehand.  tol > 0 /
+// max_it > 0: a job whose shift falls below tol, or that has run max_it
+// iterations, parks itself (status flags bits 0 and 1).
 int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
-                   uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap, size_t acc_cap, cudaStream_t s);
+                   float tol, uint32_t max_it, uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap,
+                   size_t acc_cap, cudaStream_t s);
 int batched_blocks_per_sm(size_t smem, int* out);
 // Copies cent[1] into cent[0] for every job whose parity is 1 and resets the
 // parity, so the caller's centroid arrays hold the current centroids.
 int launch_batch_sync(const BatchJobDev* jobs, uint32_t num_jobs, cudaStream_t s);
+
+// Batches over job state owned by the caller (the serving loop keeps each
+// job's buffers, scratch and status for its whole life): the job table is
+// replaced and the schedule rebuilt each round; the batch allocates only its
+// table, work list and counter.
+int batch_create_external(::ckm_batch** out);
+int batch_set_jobs(::ckm_batch* b, const BatchJobDev* jobs, uint32_t num_jobs, uint32_t tile, uint32_t ctas_per_sm,
+                   float tol, uint32_t max_it, cudaStream_t s);
+int batch_launch_step(::ckm_batch* b, cudaStream_t s);
 
 }  // namespace ckm

@@ -272,6 +272,9 @@ typedef struct ckm_batch_options {
     uint32_t ctas_per_sm;   /* 0 = choose */
     uint32_t flush_tiles;   /* tiles between FP64 merges of a CTA's partial sums; 0 = 16 */
     int autotune;           /* time candidate tile sizes / CTA counts on the batch itself */
+    float tolerance;        /* > 0: a job stops (is skipped by later steps) once its relative centroid
+                               shift falls below this (the kmeans.converge test) */
+    uint32_t max_iterations;/* > 0: a job stops after this many iterations */
 } ckm_batch_options;
 
 typedef struct ckm_batch ckm_batch;

@@ -116,3 +116,34 @@ def test_batch_rejects_bad_jobs(ckm, cuda):
         ckm.Batch([dict(points=t, centroids=t, labels=t, masses=t, n=4, d=0, k=2)])
     with pytest.raises(ckm.CkmError):
         ckm.Batch([])
+
+
+def test_batch_convergence_stop(ckm, oracle, cuda):
+    """tolerance / max_iterations: every job parks itself after the first
+    iteration whose relative centroid shift is below the tolerance (or after
+    max_iterations), exactly as if it had run alone with that stopping rule;
+    later steps leave it untouched."""
+    import torch
+    from test_pipelines_gpu import _e2e_check
+    shapes = [(4000, 2, 4), (6000, 8, 12), (3000, 3, 5), (8000, 16, 20), (2000, 32, 16), (5000, 4, 6)]
+    jobs, host = make_jobs(cuda, oracle, shapes, seed=7)
+    init = [oracle.first_x_f32(P, j["n"], j["d"], j["k"]) for j, P in zip(jobs, host)]
+    b = ckm.Batch(jobs, tolerance=1e-4, max_iterations=25)
+    try:
+        for _ in range(40):
+            b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        sh, its = b.status()
+        assert np.all(its >= 1) and np.all(its <= 25)
+        assert np.any(its < 25), "some jobs converge before the cap"
+        for i, (j, P, C0) in enumerate(zip(jobs, host, init)):
+            n, d, k = j["n"], j["d"], j["k"]
+            if its[i] < 25:
+                assert sh[i] < 1e-4
+            C = j["centroids"].cpu().numpy()
+            L = j["labels"][:n].cpu().numpy().view(np.uint32)
+            M = j["masses"].cpu().numpy().view(np.uint32)
+            _e2e_check(oracle, P, n, d, k, int(its[i]), C0, C, M, L)
+    finally:
+        b.close()
