@@ -499,3 +499,100 @@ def generate_mixture_ex(points, n, d, blobs, seed, center=("uniform", -10.0, 10.
                        1 if sigma[0] == "loguniform" else 0, sigma[1], sigma[2], 1 if dirichlet else 0)
     check(fn(ctypes.byref(spec), n, first_point, _p(points), n if stride is None else stride, _stream(stream)),
           "ckm_generate_mixture_ex_f32")
+
+
+# ----------------------------------------------------------------------------
+# Serving (ckm_server_*)
+# ----------------------------------------------------------------------------
+class ServerOptions(ctypes.Structure):
+    """struct ckm_server_options (include/ckm.h)."""
+    _fields_ = [("device", ctypes.c_int), ("device_budget_bytes", ctypes.c_uint64), ("tolerance", ctypes.c_float),
+                ("max_iterations", ctypes.c_uint32), ("round_iterations", ctypes.c_uint32),
+                ("large_work", ctypes.c_uint64)]
+
+
+class ServerJob(ctypes.Structure):
+    """struct ckm_server_job (include/ckm.h)."""
+    _fields_ = [("points", ctypes.c_void_p), ("init_centroids", ctypes.c_void_p), ("centroids", ctypes.c_void_p),
+                ("masses", ctypes.c_void_p), ("labels", ctypes.c_void_p), ("num_points", ctypes.c_uint64),
+                ("num_features", ctypes.c_uint32), ("num_clusters", ctypes.c_uint32), ("tag", ctypes.c_uint64)]
+
+
+class ServerResult(ctypes.Structure):
+    """struct ckm_server_result (include/ckm.h)."""
+    _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int), ("iterations", ctypes.c_uint32),
+                ("converged", ctypes.c_uint32), ("shift", ctypes.c_float), ("lane", ctypes.c_uint32),
+                ("latency_ns", ctypes.c_uint64)]
+
+
+_SERVER_SIGS = {
+    "ckm_server_create": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ckm_server_submit": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "ckm_server_poll": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "ckm_server_drain": ([ctypes.c_void_p], ctypes.c_int),
+    "ckm_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
+}
+EXPORTS += list(_SERVER_SIGS)
+
+
+def _server_lib():
+    L = lib()
+    if not getattr(L, "_server_sigs", False):
+        for name, (args, res) in _SERVER_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        L._server_sigs = True
+    return L
+
+
+class Server:
+    """ckm_server_*: a serving loop over host arrays.  submit() takes flat
+    column-major float32 numpy arrays (points n*d, initial centroids k*d) and
+    keeps them, and the result arrays it allocates, alive until the job's
+    result is polled."""
+
+    def __init__(self, device=0, device_budget_bytes=0, tolerance=0.0, max_iterations=0, round_iterations=0,
+                 large_work=0):
+        import numpy as np
+        self._np = np
+        L = _server_lib()
+        opt = ServerOptions(device, device_budget_bytes, tolerance, max_iterations, round_iterations, large_work)
+        h = ctypes.c_void_p()
+        check(L.ckm_server_create(ctypes.byref(opt), ctypes.byref(h)), "ckm_server_create")
+        self.h = h
+        self._live = {}
+
+    def submit(self, points, init, n, d, k, tag, labels=True, out=None):
+        np = self._np
+        if out is None:
+            out = (np.empty(k * d, np.float32), np.empty(k, np.uint32), np.empty(n, np.uint32) if labels else None)
+        C, M, Lb = out
+        job = ServerJob(points.ctypes.data, init.ctypes.data, C.ctypes.data, M.ctypes.data,
+                        Lb.ctypes.data if Lb is not None else None, n, d, k, tag)
+        self._live[tag] = (points, init, C, M, Lb)
+        rc = _server_lib().ckm_server_submit(self.h, ctypes.byref(job))
+        if rc != 0:
+            del self._live[tag]
+        check(rc, "ckm_server_submit")
+
+    def poll(self, max_results=4096):
+        arr = (ServerResult * max_results)()
+        cnt = ctypes.c_uint32()
+        check(_server_lib().ckm_server_poll(self.h, ctypes.cast(arr, ctypes.c_void_p), max_results,
+                                            ctypes.byref(cnt)), "ckm_server_poll")
+        out = []
+        for i in range(cnt.value):
+            r = arr[i]
+            _, _, C, M, Lb = self._live.pop(r.tag)
+            out.append(dict(tag=r.tag, status=r.status, iterations=r.iterations, converged=r.converged,
+                            shift=r.shift, lane=r.lane, latency_ns=r.latency_ns, centroids=C, masses=M, labels=Lb))
+        return out
+
+    def drain(self):
+        check(_server_lib().ckm_server_drain(self.h), "ckm_server_drain")
+
+    def close(self):
+        if self.h:
+            _server_lib().ckm_server_destroy(self.h)
+            self.h = None

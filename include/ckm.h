@@ -361,6 +361,61 @@ int ckm_kmeans_run_f64(const ckm_run_config *config, uint32_t max_iterations,
                        const double *host_points, double *host_centroids, uint64_t *host_masses,
                        uint64_t *host_labels, ckm_run_info *info);
 
+/* ---------------------------------------------------------------------- */
+/* Serving: a stream of independent k-means jobs (continuous batching).    */
+/* No counterpart in the reference (one problem per bench invocation).     */
+/* Jobs are submitted from any thread with host arrays; a worker thread    */
+/* admits them into device memory within a budget, advances every admitted */
+/* job by batched launches (ckm_batch_*) in rounds of a few iterations,    */
+/* retires each job at its own stopping iteration (relative centroid shift */
+/* below the tolerance, or the iteration cap) and copies its results back. */
+/* Jobs with n*k*d at or above large_work run one at a time in a second    */
+/* lane, on the tensor cores (ckm_tc_fused_f32) when eligible.             */
+/* ---------------------------------------------------------------------- */
+typedef struct ckm_server ckm_server;
+
+typedef struct ckm_server_options {
+    int device;                    /* CUDA device ordinal */
+    uint64_t device_budget_bytes;  /* device memory for admitted jobs (0 = half of the free memory) */
+    float tolerance;               /* stop once the relative centroid shift is below (0 = 1e-4) */
+    uint32_t max_iterations;       /* ... or after this many iterations (0 = 50) */
+    uint32_t round_iterations;     /* batched iterations between admissions and retirements (0 = 4) */
+    uint64_t large_work;           /* n*k*d from which a job runs in the large-job lane (0 = 2^33) */
+} ckm_server_options;
+
+typedef struct ckm_server_job {
+    const float *points;           /* host, column-major n x d; must stay valid until the job completes */
+    const float *init_centroids;   /* host, column-major k x d */
+    float *centroids;              /* host out, k x d */
+    uint32_t *masses;              /* host out, k */
+    uint32_t *labels;              /* host out, n; NULL: labels are not returned */
+    uint64_t num_points;
+    uint32_t num_features;
+    uint32_t num_clusters;
+    uint64_t tag;                  /* the caller's identifier, returned with the result */
+} ckm_server_job;
+
+typedef struct ckm_server_result {
+    uint64_t tag;
+    int status;                    /* CKM_OK, or why the job failed */
+    uint32_t iterations;
+    uint32_t converged;            /* 1: stopped on the tolerance; 0: on the iteration cap */
+    float shift;                   /* relative centroid shift of the last iteration */
+    uint32_t lane;                 /* 0: batched lane; 1: large-job lane on the tensor cores; 2: large-job lane, SIMT */
+    uint64_t latency_ns;           /* submit -> results in the caller's host arrays */
+} ckm_server_result;
+
+int ckm_server_create(const ckm_server_options *options, ckm_server **out);
+/* Queues a job (copies the descriptor, not the arrays); thread-safe. */
+int ckm_server_submit(ckm_server *server, const ckm_server_job *job);
+/* Results of the jobs completed since the last poll, oldest first (at most
+ * max_results; *count receives how many); never blocks. */
+int ckm_server_poll(ckm_server *server, ckm_server_result *results, uint32_t max_results, uint32_t *count);
+/* Blocks until every job submitted so far has completed. */
+int ckm_server_drain(ckm_server *server);
+/* Drains, stops the worker threads and frees everything. */
+int ckm_server_destroy(ckm_server *server);
+
 /* Host <-> device link probe (the roofline of the buffered pipelines, whose
  * points cross this link every iteration).  Times `repeat` back-to-back
  * copies of chunk_bytes between host memory (pinned != 0: page-locked,
