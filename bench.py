@@ -344,6 +344,144 @@ def measured_bf16_peak():
     return 1900.0, "fallback"
 
 
+def run_serving_workload(args, ckm, torch, dev):
+    """Served stream (config 5, scaled to what one GB300 and its host link
+    carry): Poisson arrivals of config-4-shaped jobs (n log-U[2^10, 2^18],
+    d in {2, 8, 32, 64}, k log-U[4, 256], k <= n/16) at --serve-rate jobs/s
+    for --serve-seconds, plus large jobs (n = 2^22, d = 128, k = 1024) at
+    --serve-large-rate jobs/s; every job stops at relative centroid shift
+    < 1e-4 or 50 iterations.  Payloads come from pools generated once and held
+    in pinned host memory.  Reports throughput and p50/p99 latency under the
+    stream, the burst capacity of the batched lane, and a plain per-job loop
+    (ckm_kmeans_run with convergence, one job at a time) on the same jobs."""
+    rng = np.random.default_rng(2024)
+    tol, cap = 1e-4, 50
+    # small-job pool
+    pool = []
+    for i in range(args.serve_pool):
+        n = int(round(np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 18)))))
+        d = int(rng.choice([2, 8, 32, 64]))
+        k = int(round(np.exp(rng.uniform(np.log(4), np.log(256)))))
+        k = max(1, min(k, n // 16))
+        P = torch.empty(n * d, dtype=torch.float32, device=dev)
+        ckm.generate_mixture(P, n, d, k, 5000 + i, sigma=(1.0, 1.0))
+        hp = torch.empty(n * d, dtype=torch.float32, pin_memory=True)
+        hp.copy_(P)
+        C0 = np.ascontiguousarray(hp.numpy().reshape(d, n)[:, :k]).reshape(-1)
+        pool.append((hp, hp.numpy(), C0, n, d, k))
+        del P
+    large = []
+    if args.serve_large_rate > 0:
+        for i in range(2):
+            n, d, k = 1 << 22, 128, 1024
+            P = torch.empty(n * d, dtype=torch.float32, device=dev)
+            ckm.generate_mixture_ex(P, n, d, k, 9000 + i, center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0),
+                                    dirichlet=True)
+            hp = torch.empty(n * d, dtype=torch.float32, pin_memory=True)
+            hp.copy_(P)
+            C0 = np.ascontiguousarray(hp.numpy().reshape(d, n)[:, :k]).reshape(-1)
+            large.append((hp, hp.numpy(), C0, n, d, k))
+            del P
+    torch.cuda.synchronize()
+
+    def submit(S, item, tag):
+        _, P, C0, n, d, k = item
+        S.submit(P, C0, n, d, k, tag)
+
+    def stream(lam, lam_l, T, seed):
+        r2 = np.random.default_rng(seed)
+        arrivals = []
+        t = 0.0
+        while True:
+            t += r2.exponential(1.0 / lam)
+            if t > T:
+                break
+            arrivals.append((t, 0))
+        t = 0.0
+        while lam_l > 0:
+            t += r2.exponential(1.0 / lam_l)
+            if t > T:
+                break
+            arrivals.append((t, 1))
+        arrivals.sort()
+        S = ckm.Server(tolerance=tol, max_iterations=cap, large_work=1 << 33, round_iterations=args.serve_round)
+        results = []
+        t0 = time.perf_counter()
+        for i, (ta, kind) in enumerate(arrivals):
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            item = large[i % len(large)] if kind else pool[i % len(pool)]
+            submit(S, item, i)
+            if i % 64 == 0:
+                results += S.poll()
+        S.drain()
+        t_end = time.perf_counter() - t0
+        while True:
+            more = S.poll()
+            if not more:
+                break
+            results += more
+        S.close()
+        ok = [r for r in results if r["status"] == 0]
+        lat_s = np.array([r["latency_ns"] for r in ok if r["lane"] == 0]) / 1e6
+        lat_l = np.array([r["latency_ns"] for r in ok if r["lane"] != 0]) / 1e6
+        its = np.array([r["iterations"] for r in ok if r["lane"] == 0])
+        pct = lambda a, q: float(np.percentile(a, q)) if a.size else None
+        return {"offered_small_per_s": lam, "offered_large_per_s": lam_l, "seconds": T, "offered_jobs": len(arrivals),
+                "completed_ok": len(ok), "failed": len(results) - len(ok), "jobs_per_s": len(ok) / t_end,
+                "latency_ms_small": {"p50": pct(lat_s, 50), "p99": pct(lat_s, 99)},
+                "latency_ms_large": {"p50": pct(lat_l, 50), "p99": pct(lat_l, 99), "count": int(lat_l.size)},
+                "iterations_small_mean": float(its.mean()) if its.size else None,
+                "converged_fraction_small": float(np.mean([r["converged"] for r in ok if r["lane"] == 0]))
+                if its.size else None}
+
+    # 2. burst capacity of the batched lane: the whole small pool, 4 times over, at once
+    S = ckm.Server(tolerance=tol, max_iterations=cap, large_work=1 << 33, round_iterations=args.serve_round)
+    nb = 4 * len(pool)
+    tb = time.perf_counter()
+    for i in range(nb):
+        submit(S, pool[i % len(pool)], i)
+        if i % 256 == 0:
+            S.poll()
+    S.drain()
+    burst_s = time.perf_counter() - tb
+    while S.poll():
+        pass
+    burst_stats = S.stats()
+    S.close()
+
+    # 3. plain per-job loop on the same small jobs (public host-level call)
+    nplain = min(len(pool), args.serve_plain_jobs)
+    tp = time.perf_counter()
+    for i in range(nplain):
+        _, P, C0, n, d, k = pool[i]
+        ckm.kmeans_run(P, d, k, cap, C0, converge=True, tolerance=tol)
+    plain_s = (time.perf_counter() - tp) / nplain
+
+    cap_rate = nb / burst_s
+    spec = stream(args.serve_rate, args.serve_large_rate, args.serve_seconds, 7)
+    sustain = stream(0.7 * cap_rate, args.serve_large_rate, args.serve_seconds, 8)
+    line = {
+        "metric": "jobs/s", "value": spec["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": spec["offered_jobs"],
+        "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (large jobs: fp16 tensor-core distances, exact FP32 labels)",
+        "data": "synthetic (seeded mixtures, pinned host payload pools)",
+        "config": {"workload": "served_stream", "seconds": args.serve_seconds, "small_rate_per_s": args.serve_rate,
+                   "large_rate_per_s": args.serve_large_rate, "small_pool": len(pool), "tolerance": tol,
+                   "max_iterations": cap, "round_iterations": args.serve_round or 4},
+        "stream_at_config_rate": spec,
+        "stream_at_70pct_capacity": sustain,
+        "burst_capacity_small_jobs_per_s": cap_rate,
+        "burst_lane_stats": dict(burst_stats, wall_ns=int(burst_s * 1e9)),
+        "plain_per_job_loop": {"jobs_per_s": 1.0 / plain_s, "jobs": nplain,
+                               "call": "ckm_kmeans_run_f32(single_stage, converge) per job"},
+        "capacity_vs_plain_loop": cap_rate * plain_s,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_tensor_core_workload(args, ckm, torch, dev):
     """Tensor-core labeling with precision recovery: n = 2^24, d = 128,
     k = 1024, a 1024-component mixture (centres ~ N(0, 4 I), sigma
@@ -445,7 +583,13 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving: small jobs per second")
+    ap.add_argument("--serve-large-rate", type=float, default=0.5, help="serving: large jobs per second")
+    ap.add_argument("--serve-pool", type=int, default=512, help="serving: distinct small-job payloads")
+    ap.add_argument("--serve-plain-jobs", type=int, default=300)
+    ap.add_argument("--serve-round", type=int, default=0, help="serving: batched iterations per round (0 = library default)")
     ap.add_argument("--jobs", type=int, default=4096, help="batched workload: number of jobs")
     ap.add_argument("--tc-points", type=int, default=0, help="tensor_core workload: points (default 2^24)")
     ap.add_argument("--no-simt-compare", action="store_true")
@@ -458,12 +602,13 @@ def main():
     if args.impl == "reference":
         return run_reference_arm(args, workload if workload in WORKLOADS else DEFAULT_WORKLOAD)
 
-    if workload in ("batched", "tensor_core"):
+    if workload in ("batched", "tensor_core", "serving"):
         import importlib
 
         import torch
         ckm = importlib.import_module("cl-kmeans_gb300")
-        run = run_batched_workload if workload == "batched" else run_tensor_core_workload
+        run = {"batched": run_batched_workload, "tensor_core": run_tensor_core_workload,
+               "serving": run_serving_workload}[workload]
         return run(args, ckm, torch, torch.device("cuda", 0))
 
     import importlib

@@ -522,7 +522,7 @@ class ServerResult(ctypes.Structure):
     """struct ckm_server_result (include/ckm.h)."""
     _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int), ("iterations", ctypes.c_uint32),
                 ("converged", ctypes.c_uint32), ("shift", ctypes.c_float), ("lane", ctypes.c_uint32),
-                ("latency_ns", ctypes.c_uint64)]
+                ("latency_ns", ctypes.c_uint64), ("error", ctypes.c_char * 128)]
 
 
 _SERVER_SIGS = {
@@ -530,6 +530,7 @@ _SERVER_SIGS = {
     "ckm_server_submit": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ckm_server_poll": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
     "ckm_server_drain": ([ctypes.c_void_p], ctypes.c_int),
+    "ckm_server_stats_get": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ckm_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
 }
 EXPORTS += list(_SERVER_SIGS)
@@ -586,11 +587,19 @@ class Server:
             r = arr[i]
             _, _, C, M, Lb = self._live.pop(r.tag)
             out.append(dict(tag=r.tag, status=r.status, iterations=r.iterations, converged=r.converged,
-                            shift=r.shift, lane=r.lane, latency_ns=r.latency_ns, centroids=C, masses=M, labels=Lb))
+                            shift=r.shift, lane=r.lane, latency_ns=r.latency_ns, error=r.error.decode(errors="replace"),
+                            centroids=C, masses=M, labels=Lb))
         return out
 
     def drain(self):
         check(_server_lib().ckm_server_drain(self.h), "ckm_server_drain")
+
+    def stats(self):
+        names = ["rounds", "job_rounds", "busy_ns", "steps_gpu_ns", "admit_ns", "retire_ns", "jobs_admitted",
+                 "jobs_completed"]
+        arr = (ctypes.c_uint64 * len(names))()
+        check(_server_lib().ckm_server_stats_get(self.h, ctypes.cast(arr, ctypes.c_void_p)), "ckm_server_stats_get")
+        return dict(zip(names, list(arr)))
 
     def close(self):
         if self.h:

@@ -107,6 +107,8 @@ struct ckm_server {
     BatchStatus* h_status = nullptr;   // pinned copy
     std::vector<int> free_slots;
     ::ckm_batch* batch = nullptr;
+    cudaEvent_t ev_s0 = nullptr, ev_s1 = nullptr;
+    ckm_server_stats stats{};  // written by the batched lane under mu
 };
 
 namespace {
@@ -120,6 +122,11 @@ void finish(ckm_server* S, SJob* j, int status, uint32_t its, uint32_t conv, flo
     r.shift = shift;
     r.lane = lane;
     r.latency_ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - j->t_submit).count();
+    std::memset(r.error, 0, sizeof(r.error));
+    if (status != CKM_OK) {  // the lane's thread set the message
+        const char* m = ckm_last_error();
+        std::strncpy(r.error, (m && *m) ? m : ckm_status_string(status), sizeof(r.error) - 1);
+    }
     {
         std::lock_guard<std::mutex> g(S->mu);
         S->results.push_back(r);
@@ -201,6 +208,7 @@ void small_lane(ckm_server* S) {
                 admit.push_back(j);
             }
         }
+        const auto t_admit = Clock::now();
         for (SJob* j : admit) {
             const int st = admit_small(S, j);
             if (st) {
@@ -214,7 +222,9 @@ void small_lane(ckm_server* S) {
             cudaEventRecord(S->ev_up, S->s_up);
             cudaStreamWaitEvent(S->s_comp, S->ev_up, 0);
         }
+        const uint64_t admit_ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t_admit).count();
         if (active.empty()) continue;
+        const auto t_round = Clock::now();
 
         // one round over every admitted job
         dev.resize(active.size());
@@ -239,7 +249,9 @@ void small_lane(ckm_server* S) {
             max_slot = std::max(max_slot, j->slot);
         }
         int st = batch_set_jobs(S->batch, dev.data(), (uint32_t)dev.size(), 1024, 2, tol, max_it, S->s_comp);
+        cudaEventRecord(S->ev_s0, S->s_comp);
         for (uint32_t r = 0; r < rounds && st == CKM_OK; ++r) st = batch_launch_step(S->batch, S->s_comp);
+        cudaEventRecord(S->ev_s1, S->s_comp);
         cudaError_t e = cudaSuccess;
         if (st == CKM_OK) {
             e = cudaMemcpyAsync(S->h_status, S->d_status, (size_t)(max_slot + 1) * sizeof(BatchStatus),
@@ -256,6 +268,9 @@ void small_lane(ckm_server* S) {
             active.clear();
             continue;
         }
+        float steps_ms = 0.f;
+        cudaEventElapsedTime(&steps_ms, S->ev_s0, S->ev_s1);
+        const auto t_retire = Clock::now();
         // retire the jobs that stopped in this round
         std::vector<SJob*> keep, done;
         for (SJob* j : active) {
@@ -281,6 +296,19 @@ void small_lane(ckm_server* S) {
             release_small(S, j, S->s_comp);
             finish(S, j, e == cudaSuccess ? CKM_OK : cuda_fail(e, "server: results"), b.iterations,
                    (tol > 0.f && b.shift < tol) ? 1u : 0u, b.shift, 0);
+        }
+        const auto t_end = Clock::now();
+        {
+            std::lock_guard<std::mutex> g(S->mu);
+            ckm_server_stats& x = S->stats;
+            x.rounds += 1;
+            x.job_rounds += active.size();
+            x.busy_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t_end - t_round).count();
+            x.steps_gpu_ns += (uint64_t)(steps_ms * 1e6);
+            x.admit_ns += admit_ns;
+            x.retire_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t_end - t_retire).count();
+            x.jobs_admitted += admit.size();
+            x.jobs_completed += done.size();
         }
         active.swap(keep);
     }
@@ -441,7 +469,8 @@ int ckm_server_create(const ckm_server_options* options, ckm_server** out) {
     if ((e = cudaStreamCreateWithFlags(&S->s_up, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S->s_comp, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S->s_large, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&S->ev_up, cudaEventDisableTiming)) != cudaSuccess)
+        (e = cudaEventCreateWithFlags(&S->ev_up, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreate(&S->ev_s0)) != cudaSuccess || (e = cudaEventCreate(&S->ev_s1)) != cudaSuccess)
         return cuda_fail(e, "server: streams");
     if ((e = cudaMalloc(&S->d_status, SLOTS * sizeof(BatchStatus))) != cudaSuccess ||
         (e = cudaMalloc(&S->d_tickets, SLOTS * sizeof(unsigned int))) != cudaSuccess ||
@@ -499,6 +528,13 @@ int ckm_server_poll(ckm_server* S, ckm_server_result* results, uint32_t max_resu
     return CKM_OK;
 }
 
+int ckm_server_stats_get(ckm_server* S, ckm_server_stats* out) {
+    if (!S || !out) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> g(S->mu);
+    *out = S->stats;
+    return CKM_OK;
+}
+
 int ckm_server_drain(ckm_server* S) {
     if (!S) return fail(CKM_ERR_INVALID_ARGUMENT, "server is NULL");
     std::unique_lock<std::mutex> lk(S->mu);
@@ -523,6 +559,8 @@ int ckm_server_destroy(ckm_server* S) {
     cudaFree(S->d_tickets);
     cudaFreeHost(S->h_status);
     cudaEventDestroy(S->ev_up);
+    cudaEventDestroy(S->ev_s0);
+    cudaEventDestroy(S->ev_s1);
     cudaStreamDestroy(S->s_up);
     cudaStreamDestroy(S->s_comp);
     cudaStreamDestroy(S->s_large);

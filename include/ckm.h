@@ -403,6 +403,7 @@ typedef struct ckm_server_result {
     float shift;                   /* relative centroid shift of the last iteration */
     uint32_t lane;                 /* 0: batched lane; 1: large-job lane on the tensor cores; 2: large-job lane, SIMT */
     uint64_t latency_ns;           /* submit -> results in the caller's host arrays */
+    char error[128];               /* why the job failed (empty when status is CKM_OK) */
 } ckm_server_result;
 
 int ckm_server_create(const ckm_server_options *options, ckm_server **out);
@@ -413,6 +414,18 @@ int ckm_server_submit(ckm_server *server, const ckm_server_job *job);
 int ckm_server_poll(ckm_server *server, ckm_server_result *results, uint32_t max_results, uint32_t *count);
 /* Blocks until every job submitted so far has completed. */
 int ckm_server_drain(ckm_server *server);
+/* Cumulative counters of the batched lane since creation. */
+typedef struct ckm_server_stats {
+    uint64_t rounds;               /* batched rounds run */
+    uint64_t job_rounds;           /* sum over rounds of the jobs in the round */
+    uint64_t busy_ns;              /* wall time of the rounds (schedule, steps, status, retirement) */
+    uint64_t steps_gpu_ns;         /* device time of the rounds' batched launches (CUDA events) */
+    uint64_t admit_ns;             /* host time spent admitting jobs (allocation, copies enqueued) */
+    uint64_t retire_ns;            /* host time spent copying results back and releasing jobs */
+    uint64_t jobs_admitted;
+    uint64_t jobs_completed;
+} ckm_server_stats;
+int ckm_server_stats_get(ckm_server *server, ckm_server_stats *stats);
 /* Drains, stops the worker threads and frees everything. */
 int ckm_server_destroy(ckm_server *server);
 
