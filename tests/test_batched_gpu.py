@@ -147,3 +147,39 @@ def test_batch_convergence_stop(ckm, oracle, cuda):
             _e2e_check(oracle, P, n, d, k, int(its[i]), C0, C, M, L)
     finally:
         b.close()
+
+
+def test_batch_screened_labels_ties_and_nan(ckm, oracle, cuda):
+    """Duplicated centroids (exact ties: the lowest index must win) and a NaN
+    centroid (an empty cluster: never chosen) in jobs of d = 8..64: labels
+    must stay the oracle's."""
+    import torch
+    shapes = [(6000, 8, 24), (5000, 32, 40), (3000, 64, 17), (4000, 16, 64)]
+    jobs, host = make_jobs(cuda, oracle, shapes, seed=11)
+    for j in jobs:
+        d, k = j["d"], j["k"]
+        C = j["centroids"].cpu().numpy().reshape(d, k)
+        C[:, 7] = C[:, 3]        # exact duplicate
+        C[:, k - 1] = C[:, 5]    # duplicate with the higher index last
+        C[:, 10] = np.nan        # empty cluster
+        j["centroids"].copy_(torch.from_numpy(np.ascontiguousarray(C).reshape(-1)))
+    b = ckm.Batch(jobs)
+    try:
+        for it in range(2):
+            b.sync()
+            torch.cuda.synchronize()
+            Cin = [j["centroids"].cpu().numpy().copy() for j in jobs]
+            b.step()
+            b.sync()
+            torch.cuda.synchronize()
+            for j, P, C0 in zip(jobs, host, Cin):
+                n, d, k = j["n"], j["d"], j["k"]
+                lab = j["labels"][:n].cpu().numpy().view(np.uint32)
+                ref = oracle.label_f32(P, n, d, k, C0)
+                assert np.array_equal(lab, ref), (it, n, d, k, int((lab != ref).sum()))
+                if it == 0:
+                    assert not np.any(lab == 7) and not np.any(lab == 10) and not np.any(lab == k - 1)
+                assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+                check_centroids(oracle, P, n, d, k, ref, j["centroids"].cpu().numpy())
+    finally:
+        b.close()
