@@ -38,7 +38,7 @@ struct ckm_batch {
     BatchSegment* d_segs = nullptr;
     unsigned int* d_work = nullptr;        // segments claimed in the current step
     // schedule
-    uint32_t grid = 0, tile = 1024, ctas_per_sm = 1, flush = 16, segments = 0;
+    uint32_t grid = 0, tile = 1024, ctas_per_sm = 1, block = 512, flush = 16, segments = 0;
     float tol = 0.f;                      // convergence stop (0: none)
     uint32_t max_it = 0;                  // iteration cap (0: none)
     uint32_t jobs_capacity = 0;           // entries of d_jobs
@@ -103,14 +103,18 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
         need_a = std::max(need_a, ((size_t)j.num_clusters * j.num_features + j.num_clusters) * sizeof(float));
     }
     const size_t budget = std::min<size_t>(di.smem_optin - 1024, 200 * 1024) / std::max<uint32_t>(ctas_per_sm, 1);
+    // the rest holds the sum tables: one column per lane index (32 copies)
+    // where a job's table fits that way, else one copy
     size_t cent_cap = std::min(a256(need_c), budget / 2);
-    size_t acc_cap = std::min(a256(need_a), budget - cent_cap);
-    if (cent_cap < a256(need_c) && acc_cap > a256(need_a)) acc_cap = a256(need_a);
+    size_t acc_cap = std::min(a256(32 * need_a), budget - cent_cap);
+    // one CTA per SM runs 512 threads (16 warps beside the whole shared
+    // memory); two or more run 256 threads each
+    const uint32_t block = ctas_per_sm <= 1 ? 512u : 256u;
     int bps = 0;
-    int st = batched_blocks_per_sm(cent_cap + acc_cap, &bps);
+    int st = batched_blocks_per_sm(cent_cap + acc_cap, block, &bps);
     if (st) return st;
     if (bps < 1) return fail(CKM_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
-    const uint32_t cps = std::min<uint32_t>(ctas_per_sm, (uint32_t)bps);
+    const uint32_t cps = std::min<uint32_t>(std::max<uint32_t>(ctas_per_sm, 1), (uint32_t)bps);
     const uint32_t grid = (uint32_t)di.sm_count * cps;
     std::vector<BatchSegment> segs;
     std::vector<uint32_t> tiles;
@@ -131,6 +135,7 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
     b->grid = grid;
     b->tile = tile;
     b->ctas_per_sm = cps;
+    b->block = block;
     b->segments = (uint32_t)segs.size();
     b->cent_cap = cent_cap;
     b->acc_cap = acc_cap;
@@ -140,8 +145,8 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
 }
 
 int step(ckm_batch* b, cudaStream_t s) {
-    return launch_batched(b->d_jobs, b->d_segs, b->segments, b->d_work, b->tol, b->max_it, b->grid, b->tile, b->flush,
-                          b->cent_cap, b->acc_cap, s);
+    return launch_batched(b->d_jobs, b->d_segs, b->segments, b->d_work, b->tol, b->max_it, b->grid, b->block, b->tile,
+                          b->flush, b->cent_cap, b->acc_cap, s);
 }
 
 int autotune(ckm_batch* b, cudaStream_t s) {

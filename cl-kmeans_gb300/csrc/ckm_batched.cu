@@ -31,10 +31,12 @@ namespace ckm {
 
 namespace {
 
-constexpr int BT = 256;  // threads per CTA
+// threads per CTA: 256 (two or more CTAs per SM) or 512 (one CTA per SM
+// with the whole shared memory, so the largest tables stay on chip)
 
 // Shared memory per CTA: centroids [c][f] (if they fit) + sum table [f][c] +
 // mass table [c].
+template <int BT>
 __device__ __forceinline__ void stage_centroids(const BatchJobDev& J, const float* __restrict__ src, float* s_c,
                                                 bool cent_smem) {
     if (!cent_smem) return;
@@ -43,27 +45,6 @@ __device__ __forceinline__ void stage_centroids(const BatchJobDev& J, const floa
         const uint32_t c = i / d, f = i - c * d;
         s_c[i] = src[(size_t)f * k + c];
     }
-}
-
-template <int D>
-__device__ __forceinline__ uint32_t label_point_fixed(const float (&x)[D], const float* __restrict__ cs, uint32_t k) {
-    float best = FLT_MAX;
-    uint32_t lab = 0;
-    for (uint32_t c = 0; c < k; ++c) {
-        const float* cr = cs + (size_t)c * D;
-        float t = x[0] - cr[0];
-        float acc = t * t;
-#pragma unroll
-        for (int f = 1; f < D; ++f) {
-            t = x[f] - cr[f];
-            acc = fmaf(t, t, acc);
-        }
-        if (acc < best) {
-            best = acc;
-            lab = c;
-        }
-    }
-    return lab;
 }
 
 __device__ __forceinline__ uint32_t label_point_generic(const float* __restrict__ P, uint64_t n, uint64_t p,
@@ -86,12 +67,38 @@ __device__ __forceinline__ uint32_t label_point_generic(const float* __restrict_
     return lab;
 }
 
-// Labels the points of tiles [t0, t1) of one job and adds them into the
-// shared tables (or, when the tables do not fit, straight into the job's FP64
-// scratch).
-template <int D>
-__device__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
-                                float* s_sum, unsigned int* s_mass, bool acc_smem, int parity) {
+// The job's centroid buffer `parity`: a select, not an indexed access, so the
+// job record stays in registers (an indexed member would put it on the stack).
+__device__ __forceinline__ float* cent_of(const BatchJobDev& J, int parity) {
+    return parity ? J.cent[1] : J.cent[0];
+}
+
+// Where a segment adds its points (per job, by table size):
+//   ACC_LANES  shared table with one column per lane index,
+//              s_sum[(f * k + c) * 32 + lane]: lanes of a warp never meet on
+//              a word, so few clusters do not serialise the atomics;
+//   ACC_SHARED shared table s_sum[f * k + c];
+//   ACC_GLOBAL straight into the job's FP64 scratch.
+enum : int { ACC_GLOBAL = 0, ACC_SHARED = 1, ACC_LANES = 2 };
+
+__device__ __forceinline__ void add_feature(const BatchJobDev& J, float* s_sum, int acc, uint32_t f, uint32_t lab,
+                                            float v) {
+    const uint32_t k = J.k;
+    if (acc == ACC_LANES) atomicAdd(&s_sum[((size_t)f * k + lab) * 32 + (threadIdx.x & 31)], v);
+    else if (acc == ACC_SHARED) atomicAdd(&s_sum[(size_t)f * k + lab], v);
+    else atomicAdd(&J.sums[(size_t)f * k + lab], (double)v);
+}
+
+__device__ __forceinline__ void add_mass(const BatchJobDev& J, unsigned int* s_mass, int acc, uint32_t lab) {
+    if (acc == ACC_LANES) atomicAdd(&s_mass[(size_t)lab * 32 + (threadIdx.x & 31)], 1u);
+    else if (acc == ACC_SHARED) atomicAdd(&s_mass[lab], 1u);
+    else atomicAdd(&J.msum[lab], 1ull);
+}
+
+// Labels the points of tiles [t0, t1) of one job and adds them up (acc).
+template <int D, int BT>
+__device__ __forceinline__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
+                                float* s_sum, unsigned int* s_mass, int acc) {
     const uint64_t n = J.n;
     const uint32_t k = J.k;
     const float* __restrict__ P = J.points;
@@ -99,42 +106,59 @@ __device__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t0, uint32_t t1, 
         float x[D];
 #pragma unroll
         for (int f = 0; f < D; ++f) x[f] = __ldg(P + (size_t)f * n + p);
-        const uint32_t lab = label_point_fixed<D>(x, s_c, k);
+        const uint32_t lab = label_rows_exact<D>(x, s_c, k);
         J.labels[p] = lab;
-        if (acc_smem) {
 #pragma unroll
-            for (int f = 0; f < D; ++f) atomicAdd(&s_sum[(size_t)f * k + lab], x[f]);
-            atomicAdd(&s_mass[lab], 1u);
-        } else {
-#pragma unroll
-            for (int f = 0; f < D; ++f) atomicAdd(&J.sums[(size_t)f * k + lab], (double)x[f]);
-            atomicAdd(&J.msum[lab], 1ull);
-        }
+        for (int f = 0; f < D; ++f) add_feature(J, s_sum, acc, f, lab, x[f]);
+        add_mass(J, s_mass, acc, lab);
     }
-    (void)parity;
 }
 
-__device__ void run_tiles_generic(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
-                                  bool cent_smem, float* s_sum, unsigned int* s_mass, bool acc_smem, int parity) {
+template <int BT>
+__device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
+                                  bool cent_smem, float* s_sum, unsigned int* s_mass, int acc, int parity) {
     const uint64_t n = J.n;
     const uint32_t k = J.k, d = J.d;
     const float* __restrict__ P = J.points;
-    const float* gc = J.cent[parity];
+    const float* gc = cent_of(J, parity);
     for (uint64_t p = (uint64_t)t0 * tile + threadIdx.x; p < (uint64_t)t1 * tile && p < n; p += BT) {
         const uint32_t lab = label_point_generic(P, n, p, s_c, cent_smem, gc, k, d);
         J.labels[p] = lab;
-        for (uint32_t f = 0; f < d; ++f) {
-            const float v = __ldg(P + (size_t)f * n + p);
-            if (acc_smem) atomicAdd(&s_sum[(size_t)f * k + lab], v);
-            else atomicAdd(&J.sums[(size_t)f * k + lab], (double)v);
-        }
-        if (acc_smem) atomicAdd(&s_mass[lab], 1u);
-        else atomicAdd(&J.msum[lab], 1ull);
+        for (uint32_t f = 0; f < d; ++f) add_feature(J, s_sum, acc, f, lab, __ldg(P + (size_t)f * n + p));
+        add_mass(J, s_mass, acc, lab);
     }
 }
 
-__device__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s_mass) {
+// Number of 32-bit words of a segment's shared table.
+__device__ __forceinline__ size_t table_words(uint32_t k, uint32_t d, int acc) {
+    const size_t w = (size_t)k * d + k;
+    return acc == ACC_LANES ? w * 32 : (acc == ACC_SHARED ? w : 0);
+}
+
+// Merges the shared table into the job's FP64 scratch and re-zeroes it.
+template <int BT>
+__device__ __forceinline__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s_mass, int acc) {
     const uint32_t k = J.k, d = J.d;
+    if (acc == ACC_LANES) {
+        // one warp per table entry: the 32 lane columns summed with shuffles
+        const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const uint32_t kd = k * d;
+        for (uint32_t e = warp; e < kd + k; e += BT / 32) {
+            if (e < kd) {
+                float v = s_sum[(size_t)e * 32 + lane];
+                s_sum[(size_t)e * 32 + lane] = 0.f;
+                v = warp_sum_f32(v);
+                if (lane == 0 && v != 0.f) atomicAdd(&J.sums[e], (double)v);
+            } else {
+                const uint32_t c = e - kd;
+                unsigned int m = s_mass[(size_t)c * 32 + lane];
+                s_mass[(size_t)c * 32 + lane] = 0u;
+                m = __reduce_add_sync(0xffffffffu, m);
+                if (lane == 0 && m) atomicAdd(&J.msum[c], (unsigned long long)m);
+            }
+        }
+        return;
+    }
     for (uint32_t i = threadIdx.x; i < k * d; i += BT) {
         const float v = s_sum[i];
         if (v != 0.f) atomicAdd(&J.sums[i], (double)v);
@@ -148,11 +172,12 @@ __device__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s
 }
 
 // Last CTA of a job: centroids, masses, relative shift; scratch back to zero.
-__device__ void finalize_job(const BatchJobDev& J, int parity, float tol, uint32_t max_it) {
+template <int BT>
+__device__ __forceinline__ void finalize_job(const BatchJobDev& J, int parity, float tol, uint32_t max_it) {
     __shared__ float s_red[BT / 32 * 2];
     const uint32_t k = J.k, d = J.d;
-    const float* old = J.cent[parity];
-    float* out = J.cent[parity ^ 1];
+    const float* old = cent_of(J, parity);
+    float* out = cent_of(J, parity ^ 1);
     float dmax = 0.f, cmax = 0.f;
     for (uint32_t e = threadIdx.x; e < k * d; e += BT) {
         const uint32_t c = e % k;
@@ -198,6 +223,7 @@ __device__ void finalize_job(const BatchJobDev& J, int parity, float tol, uint32
     }
 }
 
+template <int BT>
 __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restrict__ jobs,
                                                      const BatchSegment* __restrict__ segs, uint32_t num_segs,
                                                      unsigned int* __restrict__ work, float tol, uint32_t max_it,
@@ -224,35 +250,36 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
         const size_t cbytes = (size_t)k * d * sizeof(float);
         const bool cent_smem = cbytes <= cent_cap;
         const size_t tbytes = ((size_t)k * d + k) * sizeof(float);
-        const bool acc_smem = tbytes <= acc_cap;
+        const int acc = tbytes * 32 <= acc_cap ? ACC_LANES : (tbytes <= acc_cap ? ACC_SHARED : ACC_GLOBAL);
         float* s_c = reinterpret_cast<float*>(smem);
         float* s_sum = reinterpret_cast<float*>(smem + cent_cap);
-        unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d);
+        unsigned int* s_mass =
+            reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d * (acc == ACC_LANES ? 32 : 1));
         __syncthreads();  // previous segment's readers of the shared tables are done
-        stage_centroids(J, J.cent[parity], s_c, cent_smem);
-        if (acc_smem) {
-            for (uint32_t i = threadIdx.x; i < k * d; i += BT) s_sum[i] = 0.f;
-            for (uint32_t c = threadIdx.x; c < k; c += BT) s_mass[c] = 0u;
+        stage_centroids<BT>(J, cent_of(J, parity), s_c, cent_smem);
+        {
+            const size_t words = table_words(k, d, acc);
+            for (size_t i = threadIdx.x; i < words; i += BT) s_sum[i] = 0.f;  // sums, then masses
         }
         __syncthreads();
         for (uint32_t t = S.tile_begin; t < S.tile_end; t += flush_tiles) {
             const uint32_t te = min(S.tile_end, t + flush_tiles);
             if (cent_smem) {
                 switch (d) {
-                    case 2: run_tiles_fixed<2>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
-                    case 4: run_tiles_fixed<4>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
-                    case 8: run_tiles_fixed<8>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
-                    case 16: run_tiles_fixed<16>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
-                    case 32: run_tiles_fixed<32>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
-                    case 64: run_tiles_fixed<64>(J, t, te, tile, s_c, s_sum, s_mass, acc_smem, parity); break;
-                    default: run_tiles_generic(J, t, te, tile, s_c, true, s_sum, s_mass, acc_smem, parity); break;
+                    case 2: run_tiles_fixed<2, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
+                    case 4: run_tiles_fixed<4, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
+                    case 8: run_tiles_fixed<8, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
+                    case 16: run_tiles_fixed<16, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
+                    case 32: run_tiles_fixed<32, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
+                    case 64: run_tiles_fixed<64, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
+                    default: run_tiles_generic<BT>(J, t, te, tile, s_c, true, s_sum, s_mass, acc, parity); break;
                 }
             } else {
-                run_tiles_generic(J, t, te, tile, s_c, false, s_sum, s_mass, acc_smem, parity);
+                run_tiles_generic<BT>(J, t, te, tile, s_c, false, s_sum, s_mass, acc, parity);
             }
-            if (acc_smem) {
+            if (acc != ACC_GLOBAL) {
                 __syncthreads();
-                flush_tables(J, s_sum, s_mass);
+                flush_tables<BT>(J, s_sum, s_mass, acc);
                 __syncthreads();
             }
         }
@@ -267,22 +294,23 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
         __syncthreads();
         if (s_last) {
             __threadfence();
-            finalize_job(J, parity, tol, max_it);
+            finalize_job<BT>(J, parity, tol, max_it);
         }
     }
 }
 
-// Raises the kernel's dynamic shared-memory limit (once per device) to the
-// opt-in maximum minus its static shared memory.
+// Raises the kernel's dynamic shared-memory limit (once per device and CTA
+// size) to the opt-in maximum minus its static shared memory.
+template <int BT>
 int ensure_batched_attr() {
     static bool attr_done[64] = {false};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && !attr_done[dev]) {
         cudaFuncAttributes fa;
-        cudaError_t e = cudaFuncGetAttributes(&fa, batched_kernel);
+        cudaError_t e = cudaFuncGetAttributes(&fa, batched_kernel<BT>);
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(batched)");
-        e = cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(batched_kernel<BT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(device_info().smem_optin - fa.sharedSizeBytes));
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batched)");
         attr_done[dev] = true;
@@ -290,30 +318,44 @@ int ensure_batched_attr() {
     return CKM_OK;
 }
 
-}  // namespace
-
-int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
-                   float tol, uint32_t max_it, uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap,
-                   size_t acc_cap, cudaStream_t s) {
+template <int BT>
+int launch_batched_t(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
+                     float tol, uint32_t max_it, uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap,
+                     size_t acc_cap, cudaStream_t s) {
     const size_t smem = cent_cap + acc_cap;
-    int st = ensure_batched_attr();
+    int st = ensure_batched_attr<BT>();
     if (st) return st;
     if (grid == 0) return CKM_OK;
     cudaError_t e0 = cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
     if (e0 != cudaSuccess) return cuda_fail(e0, "batched work counter");
-    batched_kernel<<<grid, BT, smem, s>>>(jobs, segs, num_segs, work, tol, max_it, tile, flush_tiles, cent_cap,
-                                          acc_cap);
+    batched_kernel<BT><<<grid, BT, smem, s>>>(jobs, segs, num_segs, work, tol, max_it, tile, flush_tiles, cent_cap,
+                                              acc_cap);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batched launch");
 }
 
-int batched_blocks_per_sm(size_t smem, int* out) {
-    int st = ensure_batched_attr();
+}  // namespace
+
+int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
+                   float tol, uint32_t max_it, uint32_t grid, uint32_t block, uint32_t tile, uint32_t flush_tiles,
+                   size_t cent_cap, size_t acc_cap, cudaStream_t s) {
+    if (block == 512)
+        return launch_batched_t<512>(jobs, segs, num_segs, work, tol, max_it, grid, tile, flush_tiles, cent_cap,
+                                     acc_cap, s);
+    if (block != 256) return fail(CKM_ERR_INVALID_ARGUMENT, "batched: CTA size must be 256 or 512");
+    return launch_batched_t<256>(jobs, segs, num_segs, work, tol, max_it, grid, tile, flush_tiles, cent_cap, acc_cap,
+                                 s);
+}
+
+int batched_blocks_per_sm(size_t smem, uint32_t block, int* out) {
+    if (block != 256 && block != 512) return fail(CKM_ERR_INVALID_ARGUMENT, "batched: CTA size must be 256 or 512");
+    int st = block == 512 ? ensure_batched_attr<512>() : ensure_batched_attr<256>();
     if (st) return st;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batched_kernel, BT, smem) == cudaSuccess
-               ? CKM_OK
-               : fail(CKM_ERR_CUDA, "occupancy(batched)");
+    const cudaError_t e =
+        block == 512 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batched_kernel<512>, 512, smem)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batched_kernel<256>, 256, smem);
+    return e == cudaSuccess ? CKM_OK : fail(CKM_ERR_CUDA, "occupancy(batched)");
 }
 
 }  // namespace ckm

@@ -41,10 +41,11 @@ struct BatchSegment {
 // counter *work, which the launch resets to zero beforehand.  tol > 0 /
 // max_it > 0: a job whose shift falls below tol, or that has run max_it
 // iterations, parks itself (status flags bits 0 and 1).
+// block: threads per CTA, 256 or 512.
 int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
-                   float tol, uint32_t max_it, uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap,
-                   size_t acc_cap, cudaStream_t s);
-int batched_blocks_per_sm(size_t smem, int* out);
+                   float tol, uint32_t max_it, uint32_t grid, uint32_t block, uint32_t tile, uint32_t flush_tiles,
+                   size_t cent_cap, size_t acc_cap, cudaStream_t s);
+int batched_blocks_per_sm(size_t smem, uint32_t block, int* out);
 // Copies cent[1] into cent[0] for every job whose parity is 1 and resets the
 // parity, so the caller's centroid arrays hold the current centroids.
 int launch_batch_sync(const BatchJobDev* jobs, uint32_t num_jobs, cudaStream_t s);

@@ -81,6 +81,77 @@ __device__ __forceinline__ void argmin_step2(float& best, uint32_t& lab, float a
     best = m;
 }
 
+// VW consecutive floats from shared memory in one access (VW = 4 needs a
+// 16-byte aligned address, VW = 2 an 8-byte aligned one).
+template <int VW>
+__device__ __forceinline__ void load_shared_vec(float* dst, const float* src) {
+    if constexpr (VW == 4) {
+        const float4 v = *reinterpret_cast<const float4*>(src);
+        dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
+    } else if constexpr (VW == 2) {
+        const float2 v = *reinterpret_cast<const float2*>(src);
+        dst[0] = v.x; dst[1] = v.y;
+    } else {
+        dst[0] = *src;
+    }
+}
+
+// Exact label of one point held in registers against k centroid rows
+// cs[c * D + f] in shared memory (row starts 16-byte aligned when D % 4 == 0),
+// with the reference's arithmetic: t = x_f - c_f, acc = fma(t, t, acc) in
+// feature order, strict '<' argmin from FLT_MAX and cluster 0
+// (kmeans_naive.cpp:48-63, lloyd_fused_feature_sum.cl:213-239).  Four clusters
+// run per step as independent accumulation chains, so the FMA latency of one
+// chain hides behind the other three, and one vector load brings four
+// features of a row.  The argmin consumes the four distances in cluster
+// order, which gives the sequential scan's result.
+template <int D>
+__device__ __forceinline__ uint32_t label_rows_exact(const float (&x)[D], const float* __restrict__ cs, uint32_t k) {
+    constexpr int VW = (D % 4 == 0) ? 4 : ((D % 2 == 0) ? 2 : 1);
+    constexpr int CB = 4;
+    float best = FLT_MAX;
+    uint32_t lab = 0;
+    uint32_t c = 0;
+    for (; c + CB <= k; c += CB) {
+        const float* r = cs + (size_t)c * D;
+        float acc[CB];
+#pragma unroll
+        for (int f = 0; f < D; f += VW) {
+#pragma unroll
+            for (int j = 0; j < CB; ++j) {
+                float cv[VW];
+                load_shared_vec<VW>(cv, r + j * D + f);
+#pragma unroll
+                for (int v = 0; v < VW; ++v) {
+                    const float t = x[f + v] - cv[v];
+                    acc[j] = (f + v == 0) ? t * t : fmaf(t, t, acc[j]);
+                }
+            }
+        }
+        argmin_step2(best, lab, acc[0], acc[1], c);
+        argmin_step2(best, lab, acc[2], acc[3], c + 2u);
+    }
+    for (; c < k; ++c) {
+        const float* r = cs + (size_t)c * D;
+        float acc = 0.0f;
+#pragma unroll
+        for (int f = 0; f < D; f += VW) {
+            float cv[VW];
+            load_shared_vec<VW>(cv, r + f);
+#pragma unroll
+            for (int v = 0; v < VW; ++v) {
+                const float t = x[f + v] - cv[v];
+                acc = (f + v == 0) ? t * t : fmaf(t, t, acc);
+            }
+        }
+        if (acc < best) {
+            best = acc;
+            lab = c;
+        }
+    }
+    return lab;
+}
+
 __device__ __forceinline__ float warp_sum_f32(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -161,6 +161,140 @@ int launch_generic_t(const GenericArgs<T, L, M>& a, Pass pass, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
+// Fixed-d FP32 kernel for mid-size d (32, 64).  Each thread loads its point
+// once into registers (one coalesced load per feature), labels it against the
+// centroid rows in shared memory with label_rows_exact (four independent
+// cluster chains, 128-bit row loads) and adds the registers into the CTA's
+// shared-memory table, merged once into the FP64 scratch.  The generic kernel
+// re-reads the point for every cluster and runs one dependent fma chain at a
+// time; the outputs are the same.
+// ---------------------------------------------------------------------------
+
+template <int D, Pass PASS, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    rows_kernel(const GenericArgs<float, uint32_t, uint32_t> a, const int lanes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t k = a.k;
+    const uint64_t n = a.n;
+    const uint32_t kd = k * D;
+    // lanes != 0: one table column per lane index, s_sum[(f * k + c) * 32 +
+    // lane], so the lanes of a warp never meet on a word (few clusters would
+    // otherwise serialise the shared-memory atomics); else s_sum[f * k + c]
+    const uint32_t copies = lanes ? 32u : 1u;
+    const uint32_t lane_off = lanes ? (threadIdx.x & 31u) : 0u;
+    float* s_c = reinterpret_cast<float*>(smem);  // [c * D + f]
+    float* s_sum = s_c + kd;
+    unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)kd * copies);
+
+    for (uint32_t i = threadIdx.x; i < kd; i += NT) {
+        const uint32_t c = i / D, f = i - c * D;
+        s_c[i] = a.centroids[(size_t)f * k + c];
+    }
+    if constexpr (PASS == Pass::Fused) {
+        const size_t words = ((size_t)kd + k) * copies;
+        for (size_t i = threadIdx.x; i < words; i += NT) s_sum[i] = 0.0f;  // sums, then masses
+    }
+    __syncthreads();
+
+    for (uint64_t p = (uint64_t)blockIdx.x * NT + threadIdx.x; p < n; p += (uint64_t)gridDim.x * NT) {
+        float x[D];
+#pragma unroll
+        for (int f = 0; f < D; ++f) x[f] = __ldg(a.points + (uint64_t)f * n + p);
+        const uint32_t lab = label_rows_exact<D>(x, s_c, k);
+        a.labels[p] = lab;
+        if constexpr (PASS == Pass::Fused) {
+#pragma unroll
+            for (int f = 0; f < D; ++f) atomicAdd(&s_sum[((size_t)f * k + lab) * copies + lane_off], x[f]);
+            atomicAdd(&s_mass[(size_t)lab * copies + lane_off], 1u);
+        }
+    }
+
+    if constexpr (PASS == Pass::Fused) {
+        __syncthreads();
+        if (lanes) {
+            const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            for (uint32_t e = warp; e < kd + k; e += NT / 32) {
+                if (e < kd) {
+                    const float v = warp_sum_f32(s_sum[(size_t)e * 32 + lane]);
+                    if (lane == 0 && v != 0.0f) atomicAdd(&a.scratch.sums[e], (double)v);
+                } else {
+                    const unsigned int m = __reduce_add_sync(0xffffffffu, s_mass[(size_t)(e - kd) * 32 + lane]);
+                    if (lane == 0 && m) atomicAdd(&a.scratch.masses[e - kd], (unsigned long long)m);
+                }
+            }
+        } else {
+            for (uint32_t i = threadIdx.x; i < kd; i += NT) {
+                const float v = s_sum[i];
+                if (v != 0.0f) atomicAdd(&a.scratch.sums[i], (double)v);
+            }
+            for (uint32_t i = threadIdx.x; i < k; i += NT) {
+                const unsigned int v = s_mass[i];
+                if (v) atomicAdd(&a.scratch.masses[i], (unsigned long long)v);
+            }
+        }
+        if (a.mode == CKM_MODE_DEFER) return;
+        if (last_cta_ticket(a.scratch.ctrl)) finalize_block<float, uint32_t>(D, k, a.new_centroids, a.masses, a.scratch, a.mode);
+    }
+}
+
+size_t rows_smem_bytes(uint32_t d, uint32_t k, Pass pass, bool lanes) {
+    const size_t kd = (size_t)k * d;
+    return pass == Pass::Fused ? (kd + (kd + k) * (lanes ? 32 : 1)) * sizeof(float) : kd * sizeof(float);
+}
+
+constexpr size_t ROWS_TWO_CTA_LIMIT = 110 * 1024;  // two 256-thread CTAs per SM
+constexpr size_t ROWS_LANES_LIMIT = 200 * 1024;   // lane-column tables up to this size
+
+template <int D, Pass PASS, int NT, int MINB>
+int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, int lanes, cudaStream_t s) {
+    auto kern = rows_kernel<D, PASS, NT, MINB>;
+    static std::mutex mu;
+    static bool attr_done[64] = {false};
+    const DeviceInfo& di = device_info();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+            cudaFuncAttributes fa;
+            cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(rows)");
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(di.smem_optin - fa.sharedSizeBytes));
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rows)");
+            if (dev >= 0 && dev < 64) attr_done[dev] = true;
+        }
+    }
+    int bps = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, NT, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy(rows)");
+    if (bps < 1) return fail(CKM_ERR_UNSUPPORTED, "rows: kernel does not fit on an SM");
+    const uint64_t blocks = (a.n + NT - 1) / NT;
+    uint64_t grid = std::min<uint64_t>(blocks, (uint64_t)di.sm_count * bps);
+    if (grid < 1) grid = 1;
+    kern<<<(unsigned)grid, NT, smem, s>>>(a, lanes);
+    count_launch();
+    e = cudaGetLastError();
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "rows launch");
+}
+
+template <int D, Pass PASS>
+int launch_rows_d(const GenericArgs<float, uint32_t, uint32_t>& a, cudaStream_t s) {
+    const int lanes = PASS == Pass::Fused && rows_smem_bytes(D, a.k, PASS, true) <= ROWS_LANES_LIMIT;
+    const size_t smem = rows_smem_bytes(D, a.k, PASS, lanes != 0);
+    if (smem <= ROWS_TWO_CTA_LIMIT) return launch_rows_v<D, PASS, 256, 2>(a, smem, lanes, s);
+    return launch_rows_v<D, PASS, 512, 1>(a, smem, lanes, s);
+}
+
+// Returns -1000 when the shape is not one the rows kernel takes.
+int try_launch_rows(const GenericArgs<float, uint32_t, uint32_t>& a, Pass pass, cudaStream_t s) {
+    if (pass == Pass::SumsOnly || (a.d != 32 && a.d != 64)) return -1000;
+    if (rows_smem_bytes(a.d, a.k, pass, false) + 1024 > device_info().smem_optin) return -1000;
+    if (pass == Pass::Fused) return a.d == 32 ? launch_rows_d<32, Pass::Fused>(a, s) : launch_rows_d<64, Pass::Fused>(a, s);
+    return a.d == 32 ? launch_rows_d<32, Pass::LabelOnly>(a, s) : launch_rows_d<64, Pass::LabelOnly>(a, s);
+}
+
+// ---------------------------------------------------------------------------
 // Helper kernels.
 // ---------------------------------------------------------------------------
 template <typename T, typename M>
@@ -369,6 +503,8 @@ int grid_for(uint64_t work, int block) {
 int launch_generic_f32(const FusedF32& a, Pass pass, cudaStream_t s) {
     GenericArgs<float, uint32_t, uint32_t> g{a.points, a.centroids, a.labels, a.new_centroids, a.masses,
                                              a.scratch, a.n, a.d, a.k, a.mode};
+    const int st = try_launch_rows(g, pass, s);
+    if (st != -1000) return st;
     return launch_generic_t(g, pass, s);
 }
 

@@ -269,7 +269,7 @@ typedef struct ckm_batch_job {
 
 typedef struct ckm_batch_options {
     uint32_t tile_points;   /* points per tile; 0 = choose (autotune or default) */
-    uint32_t ctas_per_sm;   /* 0 = choose */
+    uint32_t ctas_per_sm;   /* 0 = choose; 1 = one 512-thread CTA per SM, 2 or more = 256-thread CTAs */
     uint32_t flush_tiles;   /* tiles between FP64 merges of a CTA's partial sums; 0 = 16 */
     int autotune;           /* time candidate tile sizes / CTA counts on the batch itself */
     float tolerance;        /* > 0: a job stops (is skipped by later steps) once its relative centroid

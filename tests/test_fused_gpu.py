@@ -70,6 +70,14 @@ SHAPES = [
     (2047, 33, 40),
     (1000, 128, 64),
     (100, 4, 1),
+    # fixed-d rows kernel (d = 32, 64): cluster counts not a multiple of four,
+    # 256-thread and 512-thread CTAs (by table size), one cluster
+    (20011, 32, 7),
+    (9000, 64, 5),
+    (6000, 64, 300),
+    (7000, 32, 600),
+    (3000, 64, 1),
+    (4100, 32, 2),
 ]
 
 
@@ -85,7 +93,7 @@ def test_fused_one_iteration_matches_oracle(ckm, oracle, cuda, n, d, k):
 
 
 @pytest.mark.parametrize("n,d,k,iters", [(1 << 16, 4, 16, 20), (40000, 2, 10, 15), (30001, 8, 24, 10),
-                                         (20000, 20, 12, 8)])
+                                         (20000, 20, 12, 8), (16384, 64, 40, 6), (12000, 32, 13, 6)])
 def test_fused_lockstep_iterations(ckm, oracle, cuda, n, d, k, iters):
     import torch
     P = blobs(n, d, k, seed=7 * n + d)
@@ -124,6 +132,31 @@ def test_ties_pick_lowest_index_and_nan_never_wins(ckm, oracle, cuda):
     ref2 = oracle.label_f32(P, n, d, k, newC)
     assert np.array_equal(labels2, ref2)
     assert not np.any(np.isin(labels2, [3, 5]))
+
+
+@pytest.mark.parametrize("d,k", [(32, 9), (64, 6), (64, 260)])
+def test_rows_kernel_ties_nan_and_labeling(ckm, oracle, cuda, d, k):
+    """d = 32 / 64 (fixed-d rows kernel): exact ties inside and across the
+    four-cluster steps pick the lowest index, a NaN centroid never wins, and
+    the labeling pass gives the fused pass's labels."""
+    import torch
+    n = 5000
+    P = blobs(n, d, 4, seed=d + k)
+    C = oracle.first_x_f32(P, n, d, k).reshape(d, k)
+    C[:, 2] = C[:, 1]            # tie inside one step of four
+    C[:, 4] = C[:, 3]            # tie across two steps
+    C[:, k - 1] = C[:, 0]        # tie with the remainder loop (k % 4 != 0)
+    C[:, 5] = np.nan
+    C = C.reshape(-1)
+    newC, masses, labels, _ = run_fused_once(ckm, cuda, P, n, d, k, C)
+    ref = oracle.label_f32(P, n, d, k, C)
+    assert np.array_equal(labels, ref), "labels differ at %d points" % int((labels != ref).sum())
+    assert not np.any(np.isin(labels, [2, 4, 5, k - 1]))
+    assert np.array_equal(masses, oracle.mass_u32(ref, k))
+    dL = torch.zeros(n, dtype=torch.int32, device=cuda)
+    ckm.labeling(to_dev(P, cuda), to_dev(C, cuda), dL, n, d, k)
+    torch.cuda.synchronize()
+    assert np.array_equal(dL.cpu().numpy().view(np.uint32), ref)
 
 
 def test_accumulate_mode_adds_into_outputs(ckm, oracle, cuda):
