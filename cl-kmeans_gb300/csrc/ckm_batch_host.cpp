@@ -99,7 +99,7 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
     // shared-memory caps: the largest job's tables, bounded
     size_t need_c = 0, need_a = 0;
     for (const auto& j : b->jobs) {
-        need_c = std::max(need_c, (size_t)j.num_clusters * j.num_features * sizeof(float));
+        need_c = std::max(need_c, ((size_t)j.num_clusters * j.num_features + ((j.num_clusters + 3) & ~3u)) * sizeof(float));
         need_a = std::max(need_a, ((size_t)j.num_clusters * j.num_features + j.num_clusters) * sizeof(float));
     }
     const size_t budget = std::min<size_t>(di.smem_optin - 1024, 200 * 1024) / std::max<uint32_t>(ctas_per_sm, 1);

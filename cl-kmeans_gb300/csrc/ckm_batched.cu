@@ -73,32 +73,43 @@ __device__ __forceinline__ float* cent_of(const BatchJobDev& J, int parity) {
     return parity ? J.cent[1] : J.cent[0];
 }
 
-// Where a segment adds its points (per job, by table size):
-//   ACC_LANES  shared table with one column per lane index,
-//              s_sum[(f * k + c) * 32 + lane]: lanes of a warp never meet on
-//              a word, so few clusters do not serialise the atomics;
-//   ACC_SHARED shared table s_sum[f * k + c];
-//   ACC_GLOBAL straight into the job's FP64 scratch.
-enum : int { ACC_GLOBAL = 0, ACC_SHARED = 1, ACC_LANES = 2 };
-
-__device__ __forceinline__ void add_feature(const BatchJobDev& J, float* s_sum, int acc, uint32_t f, uint32_t lab,
-                                            float v) {
-    const uint32_t k = J.k;
-    if (acc == ACC_LANES) atomicAdd(&s_sum[((size_t)f * k + lab) * 32 + (threadIdx.x & 31)], v);
-    else if (acc == ACC_SHARED) atomicAdd(&s_sum[(size_t)f * k + lab], v);
-    else atomicAdd(&J.sums[(size_t)f * k + lab], (double)v);
+// Where a segment adds its points, per job by table size: a shared table of
+// `copies` (a power of two up to 32) interleaved copies of the sums,
+// s_sum[(f * k + c) * copies + (lane & (copies - 1))], and one mass column
+// s_mass[c]; or, with copies = 0, straight into the job's FP64 scratch.  A
+// shared-memory FP32 atomic add retries while other lanes of the warp hit the
+// same word (eight lanes on one word ran 7.6 times slower than eight words),
+// so the copies keep the lanes of a warp apart: with 32 copies they never
+// meet.  Integer atomics do not slow down that way, so masses keep one copy.
+__device__ __forceinline__ void add_feature(const BatchJobDev& J, float* s_sum, uint32_t copies, uint32_t f,
+                                            uint32_t lab, float v) {
+    if (copies) atomicAdd(&s_sum[((size_t)f * J.k + lab) * copies + (threadIdx.x & (copies - 1u))], v);
+    else atomicAdd(&J.sums[(size_t)f * J.k + lab], (double)v);
 }
 
-__device__ __forceinline__ void add_mass(const BatchJobDev& J, unsigned int* s_mass, int acc, uint32_t lab) {
-    if (acc == ACC_LANES) atomicAdd(&s_mass[(size_t)lab * 32 + (threadIdx.x & 31)], 1u);
-    else if (acc == ACC_SHARED) atomicAdd(&s_mass[lab], 1u);
+__device__ __forceinline__ void add_mass(const BatchJobDev& J, unsigned int* s_mass, uint32_t copies, uint32_t lab) {
+    if (copies) atomicAdd(&s_mass[lab], 1u);
     else atomicAdd(&J.msum[lab], 1ull);
 }
 
-// Labels the points of tiles [t0, t1) of one job and adds them up (acc).
+// The most copies (32, 16, ..., 1) whose table fits in `cap` bytes; 0 if none.
+__device__ __forceinline__ uint32_t table_copies(uint32_t k, uint32_t d, size_t cap) {
+    const size_t kd = (size_t)k * d;
+    for (uint32_t c = 32; c >= 1; c >>= 1)
+        if ((kd * c + k) * sizeof(float) <= cap) return c;
+    return 0;
+}
+
+// Labels the points of tiles [t0, t1) of one job and adds them up.
+// d = 8, 16, 32, 64 go through the certified screen (label_rows_screened:
+// packed dot products, exact fallback per unproved point); d = 2, 4 use the
+// exact loop directly.
+template <int D> struct Screened { static constexpr bool value = D >= 8 && D % 4 == 0; };
+
 template <int D, int BT>
-__device__ __forceinline__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
-                                float* s_sum, unsigned int* s_mass, int acc) {
+__device__ __forceinline__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile,
+                                                const float* s_c, const float* s_cn, float cm, float* s_sum,
+                                                unsigned int* s_mass, uint32_t copies) {
     const uint64_t n = J.n;
     const uint32_t k = J.k;
     const float* __restrict__ P = J.points;
@@ -106,17 +117,19 @@ __device__ __forceinline__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t
         float x[D];
 #pragma unroll
         for (int f = 0; f < D; ++f) x[f] = __ldg(P + (size_t)f * n + p);
-        const uint32_t lab = label_rows_exact<D>(x, s_c, k);
+        uint32_t lab;
+        if constexpr (Screened<D>::value) lab = label_rows_screened<D>(x, s_c, s_cn, cm, k);
+        else lab = label_rows_exact<D>(x, s_c, k);
         J.labels[p] = lab;
 #pragma unroll
-        for (int f = 0; f < D; ++f) add_feature(J, s_sum, acc, f, lab, x[f]);
-        add_mass(J, s_mass, acc, lab);
+        for (int f = 0; f < D; ++f) add_feature(J, s_sum, copies, f, lab, x[f]);
+        add_mass(J, s_mass, copies, lab);
     }
 }
 
 template <int BT>
 __device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
-                                  bool cent_smem, float* s_sum, unsigned int* s_mass, int acc, int parity) {
+                                  bool cent_smem, float* s_sum, unsigned int* s_mass, uint32_t copies, int parity) {
     const uint64_t n = J.n;
     const uint32_t k = J.k, d = J.d;
     const float* __restrict__ P = J.points;
@@ -124,45 +137,36 @@ __device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t
     for (uint64_t p = (uint64_t)t0 * tile + threadIdx.x; p < (uint64_t)t1 * tile && p < n; p += BT) {
         const uint32_t lab = label_point_generic(P, n, p, s_c, cent_smem, gc, k, d);
         J.labels[p] = lab;
-        for (uint32_t f = 0; f < d; ++f) add_feature(J, s_sum, acc, f, lab, __ldg(P + (size_t)f * n + p));
-        add_mass(J, s_mass, acc, lab);
+        for (uint32_t f = 0; f < d; ++f) add_feature(J, s_sum, copies, f, lab, __ldg(P + (size_t)f * n + p));
+        add_mass(J, s_mass, copies, lab);
     }
-}
-
-// Number of 32-bit words of a segment's shared table.
-__device__ __forceinline__ size_t table_words(uint32_t k, uint32_t d, int acc) {
-    const size_t w = (size_t)k * d + k;
-    return acc == ACC_LANES ? w * 32 : (acc == ACC_SHARED ? w : 0);
 }
 
 // Merges the shared table into the job's FP64 scratch and re-zeroes it.
 template <int BT>
-__device__ __forceinline__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s_mass, int acc) {
+__device__ __forceinline__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s_mass,
+                                             uint32_t copies) {
     const uint32_t k = J.k, d = J.d;
-    if (acc == ACC_LANES) {
-        // one warp per table entry: the 32 lane columns summed with shuffles
+    const uint32_t kd = k * d;
+    if (copies == 32) {
+        // one warp per entry: the 32 copies summed with shuffles
         const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        const uint32_t kd = k * d;
-        for (uint32_t e = warp; e < kd + k; e += BT / 32) {
-            if (e < kd) {
-                float v = s_sum[(size_t)e * 32 + lane];
-                s_sum[(size_t)e * 32 + lane] = 0.f;
-                v = warp_sum_f32(v);
-                if (lane == 0 && v != 0.f) atomicAdd(&J.sums[e], (double)v);
-            } else {
-                const uint32_t c = e - kd;
-                unsigned int m = s_mass[(size_t)c * 32 + lane];
-                s_mass[(size_t)c * 32 + lane] = 0u;
-                m = __reduce_add_sync(0xffffffffu, m);
-                if (lane == 0 && m) atomicAdd(&J.msum[c], (unsigned long long)m);
-            }
+        for (uint32_t e = warp; e < kd; e += BT / 32) {
+            float v = s_sum[(size_t)e * 32 + lane];
+            s_sum[(size_t)e * 32 + lane] = 0.f;
+            v = warp_sum_f32(v);
+            if (lane == 0 && v != 0.f) atomicAdd(&J.sums[e], (double)v);
         }
-        return;
-    }
-    for (uint32_t i = threadIdx.x; i < k * d; i += BT) {
-        const float v = s_sum[i];
-        if (v != 0.f) atomicAdd(&J.sums[i], (double)v);
-        s_sum[i] = 0.f;
+    } else {
+        for (uint32_t e = threadIdx.x; e < kd; e += BT) {
+            float* src = s_sum + (size_t)e * copies;
+            float v = 0.f;
+            for (uint32_t j = 0; j < copies; ++j) {
+                v += src[j];
+                src[j] = 0.f;
+            }
+            if (v != 0.f) atomicAdd(&J.sums[e], (double)v);
+        }
     }
     for (uint32_t c = threadIdx.x; c < k; c += BT) {
         const unsigned int m = s_mass[c];
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
                                                      uint32_t tile,
                                                      uint32_t flush_tiles, size_t cent_cap, size_t acc_cap) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ unsigned int s_last, s_unit;
+    __shared__ unsigned int s_last, s_unit, s_cn_max;
     for (;;) {
         // dynamic schedule: the next unclaimed segment (largest first)
         __syncthreads();  // every thread has read the previous s_unit
@@ -247,39 +251,45 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
         if (st.flags & 1u) continue;  // job inactive this step
         const int parity = (int)(st.parity & 1u);
         const uint32_t k = J.k, d = J.d;
-        const size_t cbytes = (size_t)k * d * sizeof(float);
+        const size_t cbytes = ((size_t)k * d + ((k + 3u) & ~3u)) * sizeof(float);  // rows + |c|^2
         const bool cent_smem = cbytes <= cent_cap;
-        const size_t tbytes = ((size_t)k * d + k) * sizeof(float);
-        const int acc = tbytes * 32 <= acc_cap ? ACC_LANES : (tbytes <= acc_cap ? ACC_SHARED : ACC_GLOBAL);
+        const uint32_t copies = table_copies(k, d, acc_cap);
         float* s_c = reinterpret_cast<float*>(smem);
+        float* s_cn = s_c + (size_t)k * d;
         float* s_sum = reinterpret_cast<float*>(smem + cent_cap);
-        unsigned int* s_mass =
-            reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d * (acc == ACC_LANES ? 32 : 1));
+        unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d * copies);
         __syncthreads();  // previous segment's readers of the shared tables are done
+        if (threadIdx.x == 0) s_cn_max = 0u;
         stage_centroids<BT>(J, cent_of(J, parity), s_c, cent_smem);
         {
-            const size_t words = table_words(k, d, acc);
+            const size_t words = copies ? (size_t)k * d * copies + k : 0;
             for (size_t i = threadIdx.x; i < words; i += BT) s_sum[i] = 0.f;  // sums, then masses
         }
         __syncthreads();
+        const bool screen = cent_smem && (d == 8 || d == 16 || d == 32 || d == 64);
+        if (screen) {
+            screen_norms(s_c, d, k, s_cn, &s_cn_max, threadIdx.x, BT);
+            __syncthreads();
+        }
+        const float cm = screen_cm(s_cn_max);
         for (uint32_t t = S.tile_begin; t < S.tile_end; t += flush_tiles) {
             const uint32_t te = min(S.tile_end, t + flush_tiles);
             if (cent_smem) {
                 switch (d) {
-                    case 2: run_tiles_fixed<2, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
-                    case 4: run_tiles_fixed<4, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
-                    case 8: run_tiles_fixed<8, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
-                    case 16: run_tiles_fixed<16, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
-                    case 32: run_tiles_fixed<32, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
-                    case 64: run_tiles_fixed<64, BT>(J, t, te, tile, s_c, s_sum, s_mass, acc); break;
-                    default: run_tiles_generic<BT>(J, t, te, tile, s_c, true, s_sum, s_mass, acc, parity); break;
+                    case 2: run_tiles_fixed<2, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 4: run_tiles_fixed<4, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 8: run_tiles_fixed<8, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 16: run_tiles_fixed<16, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 32: run_tiles_fixed<32, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 64: run_tiles_fixed<64, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    default: run_tiles_generic<BT>(J, t, te, tile, s_c, true, s_sum, s_mass, copies, parity); break;
                 }
             } else {
-                run_tiles_generic<BT>(J, t, te, tile, s_c, false, s_sum, s_mass, acc, parity);
+                run_tiles_generic<BT>(J, t, te, tile, s_c, false, s_sum, s_mass, copies, parity);
             }
-            if (acc != ACC_GLOBAL) {
+            if (copies) {
                 __syncthreads();
-                flush_tables<BT>(J, s_sum, s_mass, acc);
+                flush_tables<BT>(J, s_sum, s_mass, copies);
                 __syncthreads();
             }
         }

@@ -152,6 +152,105 @@ __device__ __forceinline__ uint32_t label_rows_exact(const float (&x)[D], const 
     return lab;
 }
 
+// Certified screen in front of label_rows_exact (D % 4 == 0).
+//
+// Score s_c = |c|^2 - 2 x.c: the dot product runs as two packed FP32 chains
+// (even and odd features, one FFMA2 per feature pair), then
+// s_c = fma(-2, dot, cn[c]); half the FMA-pipe work of the exact distance and
+// a third of its instructions.  The screen keeps the lowest score m1
+// (cluster c1) and the second lowest m2.  With r >= |x| + max_c |c|,
+//   |s_c(computed) - s_c(exact)|            <= B   = (D/2 + 4) u r^2,
+//   |reference distance - exact distance|   <= rho * exact, rho = (D + 4) u,
+// (u = 2^-24; reference distance = the sequential t = x - c, fma(t, t, acc)
+// chain, exact distance = |x|^2 + s_c in real arithmetic), so
+// m2 - m1 > T = 2B + 2 rho r^2 = (3D + 16) u r^2 proves that the reference's
+// distance to c1 is strictly below its distance to every other cluster: the
+// reference's strict '<' scan then returns c1.  T is taken as
+// (4D + 32) u r^2 (1.001) + 2^-126 (margin for the rounding of r and T and for
+// underflow).  A point that is not proved that way (near ties, exact ties,
+// NaN or infinite scores, r^2 >= 2^120 where the reference's distances could
+// reach FLT_MAX) gets label_rows_exact.  NaN centroids (cn = NaN) never
+// become m1 or m2, as they never win in the reference.
+//
+// cs: centroid rows [c * D + f] (16-byte aligned rows); cn[c] = |c|^2 rounded
+// once to FP32 (NaN for a NaN centroid); cm >= max |c| over the non-NaN
+// centroids (infinite if a centroid is infinite).
+__device__ __forceinline__ void screen_track(float s, uint32_t c, float& m1, float& m2, uint32_t& i1) {
+    const bool lt = s < m1;
+    m2 = lt ? m1 : fminf(m2, s);
+    i1 = lt ? c : i1;
+    m1 = lt ? s : m1;
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t label_rows_screened(const float (&x)[D], const float* __restrict__ cs,
+                                                        const float* __restrict__ cn, float cm, uint32_t k) {
+    static_assert(D % 4 == 0, "screened rows need D % 4 == 0");
+    constexpr int CB = 4;
+    float2 nx = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int f = 0; f < D; f += 2) nx = fma2(make_float2(x[f], x[f + 1]), make_float2(x[f], x[f + 1]), nx);
+    const float xn = sqrtf(nx.x + nx.y) * (1.0f + 0x1p-16f);
+    const float r = (xn + cm) * (1.0f + 0x1p-20f);
+    const float T = fmaf((float)(4 * D + 32) * 0x1p-24f * r, r, 0x1p-126f) * 1.001f;
+
+    float m1 = INFINITY, m2 = INFINITY;
+    uint32_t i1 = 0;
+    uint32_t c = 0;
+    for (; c + CB <= k; c += CB) {
+        const float* row = cs + (size_t)c * D;
+        float2 acc[CB];
+#pragma unroll
+        for (int j = 0; j < CB; ++j) acc[j] = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int f = 0; f < D; f += 4) {
+#pragma unroll
+            for (int j = 0; j < CB; ++j) {
+                const float4 v = *reinterpret_cast<const float4*>(row + j * D + f);
+                acc[j] = fma2(make_float2(x[f], x[f + 1]), make_float2(v.x, v.y), acc[j]);
+                acc[j] = fma2(make_float2(x[f + 2], x[f + 3]), make_float2(v.z, v.w), acc[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < CB; ++j) screen_track(fmaf(-2.0f, acc[j].x + acc[j].y, cn[c + j]), c + j, m1, m2, i1);
+    }
+    for (; c < k; ++c) {
+        const float* row = cs + (size_t)c * D;
+        float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int f = 0; f < D; f += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(row + f);
+            acc = fma2(make_float2(x[f], x[f + 1]), make_float2(v.x, v.y), acc);
+            acc = fma2(make_float2(x[f + 2], x[f + 3]), make_float2(v.z, v.w), acc);
+        }
+        screen_track(fmaf(-2.0f, acc.x + acc.y, cn[c]), c, m1, m2, i1);
+    }
+    const bool proved = (m1 < INFINITY) && (m2 - m1 > T) && (r * r < 0x1p120f);
+    if (proved) return i1;
+    return label_rows_exact<D>(x, cs, k);
+}
+
+// Prologue of the screen, run by every thread of a CTA after the centroid rows
+// are in shared memory (and followed by a barrier before use): cn[c] = |c|^2
+// (FP64 sum, one rounding) and the maximum of the non-NaN cn into *s_cn_max
+// (as float bits, which order like the non-negative floats; zero it first).
+__device__ __forceinline__ void screen_norms(const float* __restrict__ cs, uint32_t d, uint32_t k, float* cn,
+                                             unsigned int* s_cn_max, uint32_t tid, uint32_t nthreads) {
+    for (uint32_t c = tid; c < k; c += nthreads) {
+        const float* row = cs + (size_t)c * d;
+        double s = 0.0;
+        for (uint32_t f = 0; f < d; ++f) s = fma((double)row[f], (double)row[f], s);
+        const float v = (float)s;
+        cn[c] = v;
+        if (!isnan(v)) atomicMax(s_cn_max, __float_as_uint(v));
+    }
+}
+
+// cm >= max |c| from the maximum squared norm (rounded up).
+__device__ __forceinline__ float screen_cm(unsigned int cn_max_bits) {
+    return sqrtf(__uint_as_float(cn_max_bits)) * (1.0f + 0x1p-16f);
+}
+
 __device__ __forceinline__ float warp_sum_f32(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -11,6 +11,7 @@
 #include "ckm_internal.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 
 namespace ckm {
@@ -167,86 +168,103 @@ int launch_generic_t(const GenericArgs<T, L, M>& a, Pass pass, cudaStream_t s) {
 // cluster chains, 128-bit row loads) and adds the registers into the CTA's
 // shared-memory table, merged once into the FP64 scratch.  The generic kernel
 // re-reads the point for every cluster and runs one dependent fma chain at a
-// time; the outputs are the same.
+// time; the outputs are the same.  Labels come from the certified screen
+// (label_rows_screened), which falls back to the exact loop per point.
 // ---------------------------------------------------------------------------
 
 template <int D, Pass PASS, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
-    rows_kernel(const GenericArgs<float, uint32_t, uint32_t> a, const int lanes) {
+    rows_kernel(const GenericArgs<float, uint32_t, uint32_t> a, const uint32_t copies, const int screen) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t k = a.k;
     const uint64_t n = a.n;
     const uint32_t kd = k * D;
-    // lanes != 0: one table column per lane index, s_sum[(f * k + c) * 32 +
-    // lane], so the lanes of a warp never meet on a word (few clusters would
-    // otherwise serialise the shared-memory atomics); else s_sum[f * k + c]
-    const uint32_t copies = lanes ? 32u : 1u;
-    const uint32_t lane_off = lanes ? (threadIdx.x & 31u) : 0u;
+    // `copies` (a power of two up to 32) interleaved copies of the sums,
+    // s_sum[(f * k + c) * copies + (lane & (copies - 1))]: a shared-memory
+    // FP32 atomic add retries while other lanes of the warp hit the same word,
+    // and the copies keep the lanes apart (with 32 they never meet).  Masses
+    // (integer atomics, which do not slow down that way) keep one copy.
+    const uint32_t lane_off = threadIdx.x & (copies - 1u);
+    __shared__ unsigned int s_cn_max;
     float* s_c = reinterpret_cast<float*>(smem);  // [c * D + f]
-    float* s_sum = s_c + kd;
+    float* s_cn = s_c + kd;                        // |c|^2 for the screen
+    float* s_sum = s_cn + ((k + 3u) & ~3u);
     unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)kd * copies);
 
+    if (threadIdx.x == 0) s_cn_max = 0u;
     for (uint32_t i = threadIdx.x; i < kd; i += NT) {
         const uint32_t c = i / D, f = i - c * D;
         s_c[i] = a.centroids[(size_t)f * k + c];
     }
     if constexpr (PASS == Pass::Fused) {
-        const size_t words = ((size_t)kd + k) * copies;
+        const size_t words = (size_t)kd * copies + k;
         for (size_t i = threadIdx.x; i < words; i += NT) s_sum[i] = 0.0f;  // sums, then masses
     }
     __syncthreads();
+    if (screen) {
+        screen_norms(s_c, D, k, s_cn, &s_cn_max, threadIdx.x, NT);
+        __syncthreads();
+    }
+    const float cm = screen_cm(s_cn_max);
 
     for (uint64_t p = (uint64_t)blockIdx.x * NT + threadIdx.x; p < n; p += (uint64_t)gridDim.x * NT) {
         float x[D];
 #pragma unroll
         for (int f = 0; f < D; ++f) x[f] = __ldg(a.points + (uint64_t)f * n + p);
-        const uint32_t lab = label_rows_exact<D>(x, s_c, k);
+        const uint32_t lab = screen ? label_rows_screened<D>(x, s_c, s_cn, cm, k) : label_rows_exact<D>(x, s_c, k);
         a.labels[p] = lab;
         if constexpr (PASS == Pass::Fused) {
 #pragma unroll
             for (int f = 0; f < D; ++f) atomicAdd(&s_sum[((size_t)f * k + lab) * copies + lane_off], x[f]);
-            atomicAdd(&s_mass[(size_t)lab * copies + lane_off], 1u);
+            atomicAdd(&s_mass[lab], 1u);
         }
     }
 
     if constexpr (PASS == Pass::Fused) {
         __syncthreads();
-        if (lanes) {
+        if (copies == 32) {
             const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-            for (uint32_t e = warp; e < kd + k; e += NT / 32) {
-                if (e < kd) {
-                    const float v = warp_sum_f32(s_sum[(size_t)e * 32 + lane]);
-                    if (lane == 0 && v != 0.0f) atomicAdd(&a.scratch.sums[e], (double)v);
-                } else {
-                    const unsigned int m = __reduce_add_sync(0xffffffffu, s_mass[(size_t)(e - kd) * 32 + lane]);
-                    if (lane == 0 && m) atomicAdd(&a.scratch.masses[e - kd], (unsigned long long)m);
-                }
+            for (uint32_t e = warp; e < kd; e += NT / 32) {
+                const float v = warp_sum_f32(s_sum[(size_t)e * 32 + lane]);
+                if (lane == 0 && v != 0.0f) atomicAdd(&a.scratch.sums[e], (double)v);
             }
         } else {
-            for (uint32_t i = threadIdx.x; i < kd; i += NT) {
-                const float v = s_sum[i];
-                if (v != 0.0f) atomicAdd(&a.scratch.sums[i], (double)v);
+            for (uint32_t e = threadIdx.x; e < kd; e += NT) {
+                float v = 0.0f;
+                for (uint32_t j = 0; j < copies; ++j) v += s_sum[(size_t)e * copies + j];
+                if (v != 0.0f) atomicAdd(&a.scratch.sums[e], (double)v);
             }
-            for (uint32_t i = threadIdx.x; i < k; i += NT) {
-                const unsigned int v = s_mass[i];
-                if (v) atomicAdd(&a.scratch.masses[i], (unsigned long long)v);
-            }
+        }
+        for (uint32_t i = threadIdx.x; i < k; i += NT) {
+            const unsigned int v = s_mass[i];
+            if (v) atomicAdd(&a.scratch.masses[i], (unsigned long long)v);
         }
         if (a.mode == CKM_MODE_DEFER) return;
         if (last_cta_ticket(a.scratch.ctrl)) finalize_block<float, uint32_t>(D, k, a.new_centroids, a.masses, a.scratch, a.mode);
     }
 }
 
-size_t rows_smem_bytes(uint32_t d, uint32_t k, Pass pass, bool lanes) {
+size_t rows_smem_bytes(uint32_t d, uint32_t k, Pass pass, uint32_t copies) {
     const size_t kd = (size_t)k * d;
-    return pass == Pass::Fused ? (kd + (kd + k) * (lanes ? 32 : 1)) * sizeof(float) : kd * sizeof(float);
+    const size_t cent = kd + ((k + 3) & ~size_t(3));  // rows + |c|^2
+    return (pass == Pass::Fused ? cent + kd * copies + k : cent) * sizeof(float);
+}
+
+// The certified screen (label_rows_screened) is on unless the environment
+// variable CKM_SCREEN is "0" (exact arithmetic for every cluster).
+int screen_enabled() {
+    static int v = [] {
+        const char* e = getenv("CKM_SCREEN");
+        return (e && e[0] == '0') ? 0 : 1;
+    }();
+    return v;
 }
 
 constexpr size_t ROWS_TWO_CTA_LIMIT = 110 * 1024;  // two 256-thread CTAs per SM
-constexpr size_t ROWS_LANES_LIMIT = 200 * 1024;   // lane-column tables up to this size
+constexpr size_t ROWS_COPIES_LIMIT = 200 * 1024;  // tables of several copies up to this size
 
 template <int D, Pass PASS, int NT, int MINB>
-int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, int lanes, cudaStream_t s) {
+int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, uint32_t copies, cudaStream_t s) {
     auto kern = rows_kernel<D, PASS, NT, MINB>;
     static std::mutex mu;
     static bool attr_done[64] = {false};
@@ -272,7 +290,7 @@ int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, 
     const uint64_t blocks = (a.n + NT - 1) / NT;
     uint64_t grid = std::min<uint64_t>(blocks, (uint64_t)di.sm_count * bps);
     if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, NT, smem, s>>>(a, lanes);
+    kern<<<(unsigned)grid, NT, smem, s>>>(a, copies, screen_enabled());
     count_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "rows launch");
@@ -280,16 +298,23 @@ int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, 
 
 template <int D, Pass PASS>
 int launch_rows_d(const GenericArgs<float, uint32_t, uint32_t>& a, cudaStream_t s) {
-    const int lanes = PASS == Pass::Fused && rows_smem_bytes(D, a.k, PASS, true) <= ROWS_LANES_LIMIT;
-    const size_t smem = rows_smem_bytes(D, a.k, PASS, lanes != 0);
-    if (smem <= ROWS_TWO_CTA_LIMIT) return launch_rows_v<D, PASS, 256, 2>(a, smem, lanes, s);
-    return launch_rows_v<D, PASS, 512, 1>(a, smem, lanes, s);
+    // the most copies that keep the table within the limit (one at least)
+    uint32_t copies = 1;
+    if (PASS == Pass::Fused)
+        for (uint32_t c = 32; c > 1; c >>= 1)
+            if (rows_smem_bytes(D, a.k, PASS, c) <= ROWS_COPIES_LIMIT) {
+                copies = c;
+                break;
+            }
+    const size_t smem = rows_smem_bytes(D, a.k, PASS, copies);
+    if (smem <= ROWS_TWO_CTA_LIMIT) return launch_rows_v<D, PASS, 256, 2>(a, smem, copies, s);
+    return launch_rows_v<D, PASS, 512, 1>(a, smem, copies, s);
 }
 
 // Returns -1000 when the shape is not one the rows kernel takes.
 int try_launch_rows(const GenericArgs<float, uint32_t, uint32_t>& a, Pass pass, cudaStream_t s) {
     if (pass == Pass::SumsOnly || (a.d != 32 && a.d != 64)) return -1000;
-    if (rows_smem_bytes(a.d, a.k, pass, false) + 1024 > device_info().smem_optin) return -1000;
+    if (rows_smem_bytes(a.d, a.k, pass, 1) + 1024 > device_info().smem_optin) return -1000;
     if (pass == Pass::Fused) return a.d == 32 ? launch_rows_d<32, Pass::Fused>(a, s) : launch_rows_d<64, Pass::Fused>(a, s);
     return a.d == 32 ? launch_rows_d<32, Pass::LabelOnly>(a, s) : launch_rows_d<64, Pass::LabelOnly>(a, s);
 }

@@ -183,3 +183,41 @@ def test_batch_screened_labels_ties_and_nan(ckm, oracle, cuda):
                 check_centroids(oracle, P, n, d, k, ref, j["centroids"].cpu().numpy())
     finally:
         b.close()
+
+
+def test_batch_screen_fallback_offsets_and_huge_centroids(ckm, oracle, cuda):
+    """Jobs of d = 8..64 whose points sit far from the origin (many points
+    fall back from the screen to the exact loop) or that hold a huge or an
+    infinite centroid (every point falls back): labels stay the oracle's."""
+    import torch
+    shapes = [(5000, 8, 20), (4000, 16, 12), (6000, 32, 30), (3000, 64, 9), (3000, 64, 40), (2000, 32, 5)]
+    jobs, host = make_jobs(cuda, oracle, shapes, seed=13)
+    for i, j in enumerate(jobs):
+        n, d, k = j["n"], j["d"], j["k"]
+        if i < 3:
+            host[i] = (host[i] + np.float32(2500.0)).astype(np.float32)
+            j["points"].copy_(torch.from_numpy(host[i]))
+            C = oracle.first_x_f32(host[i], n, d, k).reshape(d, k)
+        else:
+            C = j["centroids"].cpu().numpy().reshape(d, k)
+            if i == 3:
+                C[:, 2] = 1e30
+            elif i == 4:
+                C[1, 3] = np.inf
+            else:
+                C[:, 1] = -1e31
+        j["centroids"].copy_(torch.from_numpy(np.ascontiguousarray(C).reshape(-1)))
+    b = ckm.Batch(jobs)
+    try:
+        Cin = [j["centroids"].cpu().numpy().copy() for j in jobs]
+        b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        for j, P, C0 in zip(jobs, host, Cin):
+            n, d, k = j["n"], j["d"], j["k"]
+            lab = j["labels"][:n].cpu().numpy().view(np.uint32)
+            ref = oracle.label_f32(P, n, d, k, C0)
+            assert np.array_equal(lab, ref), (n, d, k, int((lab != ref).sum()))
+            assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+    finally:
+        b.close()

@@ -159,6 +159,29 @@ def test_rows_kernel_ties_nan_and_labeling(ckm, oracle, cuda, d, k):
     assert np.array_equal(dL.cpu().numpy().view(np.uint32), ref)
 
 
+@pytest.mark.parametrize("d,case", [(32, "offset"), (64, "offset"), (64, "huge"), (32, "inf")])
+def test_screen_fallback_keeps_reference_labels(ckm, oracle, cuda, d, case):
+    """d = 32 / 64 label through the certified screen.  Points it cannot prove
+    are labelled with the exact loop: data far from the origin (the rounding
+    bound grows with |x| + max|c|, so many points fall back), a centroid so
+    large that (|x| + max|c|)^2 >= 2^120 (every point falls back), and an
+    infinite centroid (every point falls back; that cluster never wins)."""
+    n, k = 6000, 24
+    P = blobs(n, d, 8, seed=d + len(case))
+    if case == "offset":
+        P = (P + np.float32(3000.0)).astype(np.float32)
+    C = oracle.first_x_f32(P, n, d, k).reshape(d, k)
+    if case == "huge":
+        C[:, 4] = 1e30
+    elif case == "inf":
+        C[0, 4] = np.inf
+    C = C.reshape(-1)
+    newC, masses, labels, _ = run_fused_once(ckm, cuda, P, n, d, k, C)
+    ref = oracle.label_f32(P, n, d, k, C)
+    assert np.array_equal(labels, ref), "labels differ at %d points" % int((labels != ref).sum())
+    assert np.array_equal(masses, oracle.mass_u32(ref, k))
+
+
 def test_accumulate_mode_adds_into_outputs(ckm, oracle, cuda):
     """Reference FusedFunction contract: += into new_centroids and masses."""
     import torch
