@@ -26,6 +26,7 @@
 #include "ckm_batched.h"
 #include "ckm_device.cuh"
 #include "ckm_internal.h"
+#include "ckm_mma_screen.cuh"
 
 namespace ckm {
 
@@ -142,6 +143,43 @@ __device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t
     }
 }
 
+// d = 32 / 64 jobs with at least MMA_MIN_K clusters: 8 points per warp
+// through the tensor-core screen (mma_label8), then each lane adds its
+// quarter of its point's features into the table.
+constexpr uint32_t MMA_MIN_K = 16;
+
+// Shared bytes of the MMA centroid fragments plus |c|^2 (16-byte multiple).
+__host__ __device__ __forceinline__ size_t mma_cent_bytes(uint32_t k, uint32_t d) {
+    const size_t k_pad = mma_k_pad(k);
+    return ((k_pad * d * 2 + k_pad) * sizeof(float) + 15) & ~size_t(15);
+}
+
+template <int D, int BT>
+__device__ __forceinline__ void run_tiles_mma(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile,
+                                              const float4* frag, const float* s_cn, float cm, float* s_sum,
+                                              unsigned int* s_mass, uint32_t copies) {
+    const uint64_t n = J.n;
+    const uint32_t k = J.k;
+    const uint64_t begin = (uint64_t)t0 * tile;
+    const uint64_t end = min((uint64_t)t1 * tile, n);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3u;
+#pragma unroll 1
+    for (uint64_t p0 = begin + (uint64_t)warp * 8; p0 < end; p0 += (uint64_t)(BT / 32) * 8) {
+        uint32_t bh[D / 4], bm[D / 4];
+        uint32_t lab;
+        mma_label8<D>(J.points, n, p0, end, frag, s_cn, cm, k, bh, bm, lab);
+        if (p0 + g < end) {
+            if (t == 0) J.labels[p0 + g] = lab;
+#pragma unroll
+            for (uint32_t i = 0; i < (uint32_t)D / 4; ++i) {
+                const uint32_t f = (i >> 1) * 8 + t + ((i & 1u) ? 4u : 0u);
+                add_feature(J, s_sum, copies, f, lab, __uint_as_float(bh[i]) + __uint_as_float(bm[i]));  // x exactly
+            }
+            if (t == 0) add_mass(J, s_mass, copies, lab);
+        }
+    }
+}
+
 // Merges the shared table into the job's FP64 scratch and re-zeroes it.
 template <int BT>
 __device__ __forceinline__ void flush_tables(const BatchJobDev& J, float* s_sum, unsigned int* s_mass,
@@ -228,7 +266,7 @@ __device__ __forceinline__ void finalize_job(const BatchJobDev& J, int parity, f
 }
 
 template <int BT>
-__global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restrict__ jobs,
+__global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev* __restrict__ jobs,
                                                      const BatchSegment* __restrict__ segs, uint32_t num_segs,
                                                      unsigned int* __restrict__ work, float tol, uint32_t max_it,
                                                      uint32_t tile,
@@ -251,16 +289,28 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
         if (st.flags & 1u) continue;  // job inactive this step
         const int parity = (int)(st.parity & 1u);
         const uint32_t k = J.k, d = J.d;
+        // shared memory of this segment: centroids (MMA fragments, or rows for
+        // the SIMT screen / exact loop, or none) at the start, the sum table
+        // in the rest
+        const size_t total = cent_cap + acc_cap;
+        const bool mma = (d == 32 || d == 64) && k >= MMA_MIN_K &&
+                         mma_cent_bytes(k, d) + ((size_t)k * d + k) * sizeof(float) <= total;
         const size_t cbytes = ((size_t)k * d + ((k + 3u) & ~3u)) * sizeof(float);  // rows + |c|^2
-        const bool cent_smem = cbytes <= cent_cap;
-        const uint32_t copies = table_copies(k, d, acc_cap);
+        const bool cent_smem = !mma && cbytes <= cent_cap;
+        const size_t table_off = mma ? mma_cent_bytes(k, d) : (cent_smem ? ((cbytes + 15) & ~size_t(15)) : 0);
+        const uint32_t copies = table_copies(k, d, total - table_off);
         float* s_c = reinterpret_cast<float*>(smem);
-        float* s_cn = s_c + (size_t)k * d;
-        float* s_sum = reinterpret_cast<float*>(smem + cent_cap);
+        float* s_cn = mma ? s_c + (size_t)mma_k_pad(k) * d * 2 : s_c + (size_t)k * d;
+        float* s_sum = reinterpret_cast<float*>(smem + table_off);
         unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d * copies);
         __syncthreads();  // previous segment's readers of the shared tables are done
         if (threadIdx.x == 0) s_cn_max = 0u;
-        stage_centroids<BT>(J, cent_of(J, parity), s_c, cent_smem);
+        if (mma) {
+            if (d == 32) mma_stage_centroids<32>(cent_of(J, parity), k, reinterpret_cast<float4*>(s_c), s_cn, &s_cn_max, threadIdx.x, BT);
+            else mma_stage_centroids<64>(cent_of(J, parity), k, reinterpret_cast<float4*>(s_c), s_cn, &s_cn_max, threadIdx.x, BT);
+        } else {
+            stage_centroids<BT>(J, cent_of(J, parity), s_c, cent_smem);
+        }
         {
             const size_t words = copies ? (size_t)k * d * copies + k : 0;
             for (size_t i = threadIdx.x; i < words; i += BT) s_sum[i] = 0.f;  // sums, then masses
@@ -274,7 +324,10 @@ __global__ void __launch_bounds__(BT) batched_kernel(const BatchJobDev* __restri
         const float cm = screen_cm(s_cn_max);
         for (uint32_t t = S.tile_begin; t < S.tile_end; t += flush_tiles) {
             const uint32_t te = min(S.tile_end, t + flush_tiles);
-            if (cent_smem) {
+            if (mma) {
+                if (d == 32) run_tiles_mma<32, BT>(J, t, te, tile, reinterpret_cast<const float4*>(s_c), s_cn, cm, s_sum, s_mass, copies);
+                else run_tiles_mma<64, BT>(J, t, te, tile, reinterpret_cast<const float4*>(s_c), s_cn, cm, s_sum, s_mass, copies);
+            } else if (cent_smem) {
                 switch (d) {
                     case 2: run_tiles_fixed<2, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
                     case 4: run_tiles_fixed<4, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;

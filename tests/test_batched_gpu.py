@@ -186,26 +186,28 @@ def test_batch_screened_labels_ties_and_nan(ckm, oracle, cuda):
 
 
 def test_batch_screen_fallback_offsets_and_huge_centroids(ckm, oracle, cuda):
-    """Jobs of d = 8..64 whose points sit far from the origin (many points
-    fall back from the screen to the exact loop) or that hold a huge or an
-    infinite centroid (every point falls back): labels stay the oracle's."""
+    """Jobs of d = 8..64 (SIMT screen for k < 16, tensor-core screen for
+    d = 32 / 64 with k >= 16) whose points sit far from the origin (many
+    points fall back from the screen to the exact loop) or that hold a huge or
+    an infinite centroid (every point falls back): labels stay the oracle's."""
     import torch
-    shapes = [(5000, 8, 20), (4000, 16, 12), (6000, 32, 30), (3000, 64, 9), (3000, 64, 40), (2000, 32, 5)]
-    jobs, host = make_jobs(cuda, oracle, shapes, seed=13)
-    for i, j in enumerate(jobs):
-        n, d, k = j["n"], j["d"], j["k"]
-        if i < 3:
+    # (n, d, k, change)
+    cases = [(5000, 8, 20, "offset"), (4000, 64, 24, "offset"), (6000, 32, 30, "offset"), (3000, 64, 9, "huge"),
+             (3000, 64, 40, "inf"), (2000, 32, 5, "-huge"), (2500, 64, 33, "huge"), (2600, 32, 48, "inf")]
+    jobs, host = make_jobs(cuda, oracle, [c[:3] for c in cases], seed=13)
+    for i, (j, (n, d, k, change)) in enumerate(zip(jobs, cases)):
+        if change == "offset":
             host[i] = (host[i] + np.float32(2500.0)).astype(np.float32)
             j["points"].copy_(torch.from_numpy(host[i]))
             C = oracle.first_x_f32(host[i], n, d, k).reshape(d, k)
         else:
             C = j["centroids"].cpu().numpy().reshape(d, k)
-            if i == 3:
+            if change == "huge":
                 C[:, 2] = 1e30
-            elif i == 4:
-                C[1, 3] = np.inf
-            else:
+            elif change == "-huge":
                 C[:, 1] = -1e31
+            else:
+                C[1, 3] = np.inf
         j["centroids"].copy_(torch.from_numpy(np.ascontiguousarray(C).reshape(-1)))
     b = ckm.Batch(jobs)
     try:
