@@ -248,7 +248,9 @@ void small_lane(ckm_server* S) {
             J.pad = 0;
             max_slot = std::max(max_slot, j->slot);
         }
-        int st = batch_set_jobs(S->batch, dev.data(), (uint32_t)dev.size(), 1024, 2, tol, max_it, S->s_comp);
+        // one 512-thread CTA per SM with the whole shared memory (room for the
+        // tensor-core centroid fragments of d = 32 / 64 jobs), 4096-point tiles
+        int st = batch_set_jobs(S->batch, dev.data(), (uint32_t)dev.size(), 4096, 1, tol, max_it, S->s_comp);
         cudaEventRecord(S->ev_s0, S->s_comp);
         for (uint32_t r = 0; r < rounds && st == CKM_OK; ++r) st = batch_launch_step(S->batch, S->s_comp);
         cudaEventRecord(S->ev_s1, S->s_comp);
