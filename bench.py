@@ -228,8 +228,21 @@ def run_batched_workload(args, ckm, torch, dev):
     GPU.  Metric: jobs/s."""
     num_jobs, iters = args.jobs, 20
     jobs = make_batched_jobs(ckm, torch, num_jobs, 1234, dev)
+    subset = None
+    if args.batch_d or args.batch_min_k or args.batch_max_k or args.batch_max_jobs:
+        # a class of the same job list (profiling and breakdowns)
+        jobs = [j for j in jobs if (not args.batch_d or j["d"] == args.batch_d) and j["k"] >= args.batch_min_k
+                and (not args.batch_max_k or j["k"] < args.batch_max_k)]
+        if args.batch_max_jobs:
+            jobs = jobs[:args.batch_max_jobs]
+        num_jobs = len(jobs)
+        subset = {"d": args.batch_d or None, "min_k": args.batch_min_k, "max_k": args.batch_max_k or None,
+                  "of_jobs": args.jobs}
+        torch.cuda.empty_cache()
     total_pts = sum(j["n"] for j in jobs)
     stream = torch.cuda.current_stream()
+    if args.no_plain:
+        return run_batched_only(args, ckm, torch, jobs, iters, total_pts, subset, stream)
 
     # plain per-job loop (the reference's one-problem-at-a-time structure)
     scratch = {}
@@ -264,7 +277,11 @@ def run_batched_workload(args, ckm, torch, dev):
     info = batch.info()
     for j in jobs:
         j["centroids"].copy_(j["init"])
-    batch.run(iters, use_graph=True)      # capture + warm-up
+    warm = max(3, args.warmup)
+    for _ in range(warm):                 # capture + warm-up
+        for j in jobs:
+            j["centroids"].copy_(j["init"])
+        batch.run(iters, use_graph=True)
     times = []
     for _ in range(max(3, args.steps if args.steps < 20 else 5)):
         for j in jobs:
@@ -314,7 +331,7 @@ def run_batched_workload(args, ckm, torch, dev):
     batch.close()
     line = {
         "metric": "jobs/s", "value": num_jobs / batch_s, "unit": "jobs/s", "n_gpus": 1, "steps": len(times),
-        "warmup": 1, "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "warmup": warm, "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (per-job seeded Gaussian mixtures generated on the device)",
         "config": {"workload": "batched_%d_jobs" % num_jobs, "iterations": iters, "total_points": total_pts,
                    "schedule": info, "graph": True},
@@ -324,6 +341,40 @@ def run_batched_workload(args, ckm, torch, dev):
         "pts_iter_per_s": total_pts * iters / batch_s,
         "lockstep_vs_plain": {"max_rel_centroid_diff": lock_worst, "label_mismatches": lock_label_diff},
         "after_20_iterations_vs_plain": {"max_rel_centroid_diff": worst, "jobs_beyond_1e-5": diverged},
+        "gpu_launches": int(gpu_launches),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batched_only(args, ckm, torch, jobs, iters, total_pts, subset, stream):
+    """--no-plain: the batched launches alone (one step = one iteration of
+    every job, no graph), for profiling a class of jobs."""
+    batch = ckm.Batch(jobs, tile_points=4096, ctas_per_sm=1)
+    warm = max(3, args.warmup)
+    for _ in range(warm):
+        batch.step(stream)
+    torch.cuda.synchronize()
+    steps = max(1, args.steps if args.steps < 1000 else 5)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = ckm.launch_count()
+    e0.record(stream)
+    for _ in range(steps):
+        batch.step(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    gpu_launches = ckm.launch_count() - launches0
+    info = batch.info()
+    batch.close()
+    work = sum(j["n"] * j["k"] * j["d"] * 2 for j in jobs)
+    line = {
+        "metric": "pts*iter/s", "value": total_pts / (ms / 1e3), "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
+        "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (per-job seeded Gaussian mixtures generated on the device)",
+        "config": {"workload": "batched_%d_jobs_one_iteration" % len(jobs), "subset": subset,
+                   "total_points": total_pts, "schedule": info, "graph": False},
+        "exact_arithmetic_tflops": work / ms / 1e9,
         "gpu_launches": int(gpu_launches),
     }
     print(json.dumps(line), flush=True)
@@ -591,6 +642,12 @@ def main():
     ap.add_argument("--serve-plain-jobs", type=int, default=300)
     ap.add_argument("--serve-round", type=int, default=0, help="serving: batched iterations per round (0 = library default)")
     ap.add_argument("--jobs", type=int, default=4096, help="batched workload: number of jobs")
+    ap.add_argument("--batch-d", type=int, default=0, help="batched workload: keep only jobs of this d")
+    ap.add_argument("--batch-min-k", type=int, default=0, help="batched workload: keep only jobs with k >= this")
+    ap.add_argument("--batch-max-k", type=int, default=0, help="batched workload: keep only jobs with k < this")
+    ap.add_argument("--batch-max-jobs", type=int, default=0, help="batched workload: keep at most this many jobs")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="batched workload: time the batched launches alone (no plain loop, no graph)")
     ap.add_argument("--tc-points", type=int, default=0, help="tensor_core workload: points (default 2^24)")
     ap.add_argument("--no-simt-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
