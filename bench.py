@@ -381,6 +381,68 @@ def run_batched_only(args, ckm, torch, jobs, iters, total_pts, subset, stream):
     return 0
 
 
+def run_buffered_workload(args, ckm, torch, dev):
+    """Out-of-core Lloyd (config 2b, scaled to this box): n points of d = 16
+    from a 64-blob mixture (centres U[-10,10]^16, sigma U[0.5,2]) held in
+    PINNED HOST memory, k = 64, first_x initial centroids, run through the
+    buffered three-stage pipeline (ckm_kmeans_run_f32, three_stage_buffered)
+    with the device budget capped at a quarter of the point bytes (config 2b:
+    128 GiB of points, 32 GiB budget), so most chunks stream over the host
+    link every iteration.  Metric: pts*iter/s end to end (host points, device
+    compute, host labels)."""
+    n = args.buffered_points or (1 << 29)
+    d, k, blobs = 16, 64, 64
+    iters = args.buffered_iterations
+    budget = args.buffered_budget or (n * d * 4) // 4
+    # host points generated on the device in chunks of the same mixture
+    P = torch.empty(n * d, dtype=torch.float32, pin_memory=True)
+    L = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    chunk = 1 << 25
+    buf = torch.empty(chunk * d, dtype=torch.float32, device=dev)
+    Pv = P.view(d, n)
+    for p0 in range(0, n, chunk):
+        m = min(chunk, n - p0)
+        ckm.generate_mixture(buf, m, d, blobs, SEED, sigma=(0.5, 2.0), first_point=p0)
+        Pv[:, p0:p0 + m].copy_(buf[:m * d].view(d, m), non_blocking=False)
+    del buf
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    Pn, Ln = P.numpy(), L.numpy().view(np.uint32)
+    C0 = np.ascontiguousarray(Pv[:, :k].numpy()).reshape(-1)
+    link = ckm.transfer_probe(1 << 30, repeat=4, pinned=True, to_device=True, trials=2)
+
+    def run(iterations):
+        t0 = time.perf_counter()
+        C, M, Lo, info = ckm.kmeans_run(Pn, d, k, iterations, C0, pipeline="three_stage_buffered",
+                                        device_budget_bytes=budget, labels=Ln)
+        return time.perf_counter() - t0, info, M
+
+    run(1)                          # warm-up: allocations, first chunks
+    times, infos = [], []
+    steps = max(1, min(args.steps, 3))
+    for _ in range(steps):
+        t, info, M = run(iters)
+        times.append(t)
+        infos.append(info)
+    t = statistics.median(times)
+    info = infos[0]
+    assert int(M.astype(np.uint64).sum()) == n
+    line = {
+        "metric": "pts*iter/s", "value": n * iters / t, "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
+        "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded 64-blob mixture generated on the device, copied to pinned host memory)",
+        "config": {"workload": "buffered_three_stage_n%d_d%d_k%d" % (n, d, k), "n": n, "d": d, "k": k,
+                   "iterations_per_step": iters, "point_bytes": n * d * 4, "device_budget_bytes": budget,
+                   "pipeline": "three_stage_buffered", "host_memory": "pinned"},
+        "h2d_bytes_per_step": int(info.h2d_bytes), "d2h_bytes_per_step": int(info.d2h_bytes),
+        "h2d_gbs_effective": info.h2d_bytes / t / 1e9,
+        "h2d_link_probe_gbs": link[0],
+        "kernel_launches_per_step": int(info.kernel_launches),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def measured_bf16_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -634,7 +696,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core", "serving"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core", "serving", "buffered"])
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving: small jobs per second")
     ap.add_argument("--serve-large-rate", type=float, default=0.5, help="serving: large jobs per second")
@@ -649,6 +711,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true",
                     help="batched workload: time the batched launches alone (no plain loop, no graph)")
     ap.add_argument("--tc-points", type=int, default=0, help="tensor_core workload: points (default 2^24)")
+    ap.add_argument("--buffered-points", type=int, default=0, help="buffered workload: points (default 2^29)")
+    ap.add_argument("--buffered-budget", type=int, default=0,
+                    help="buffered workload: device budget in bytes (default a quarter of the point bytes)")
+    ap.add_argument("--buffered-iterations", type=int, default=5, help="buffered workload: iterations per step")
     ap.add_argument("--no-simt-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -659,13 +725,13 @@ def main():
     if args.impl == "reference":
         return run_reference_arm(args, workload if workload in WORKLOADS else DEFAULT_WORKLOAD)
 
-    if workload in ("batched", "tensor_core", "serving"):
+    if workload in ("batched", "tensor_core", "serving", "buffered"):
         import importlib
 
         import torch
         ckm = importlib.import_module("cl-kmeans_gb300")
         run = {"batched": run_batched_workload, "tensor_core": run_tensor_core_workload,
-               "serving": run_serving_workload}[workload]
+               "serving": run_serving_workload, "buffered": run_buffered_workload}[workload]
         return run(args, ckm, torch, torch.device("cuda", 0))
 
     import importlib
