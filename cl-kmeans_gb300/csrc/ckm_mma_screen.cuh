@@ -12,14 +12,20 @@
 // Bound on the score error, with r >= |x| + max|c| and u = 2^-24:
 //   split:        |x_mid.c_mid| + 2^-10 (|x_mid||c_hi| + |x_hi||c_mid|)
 //                 <= 5 * 2^-22 |x| |c|
-//   accumulation: every product term may cost 2 ulps of the running sum
-//                 (the convention of the tcgen05 path): 3D * 2^-22 |x| |c|
+//   accumulation: the three products accumulate in three chains (mid x hi,
+//                 hi x mid, hi x hi), and every product term may cost 2 ulps
+//                 of its chain's running sum (the convention of the tcgen05
+//                 path).  A chain's running sum is at most the sum of its
+//                 |terms|: D terms of the hi x hi chain sum to <= |x||c|,
+//                 each mid chain's to <= 2^-11 (1.001) |x||c|, so the chains
+//                 cost <= D (1 + 2^-9) 2^-22 |x||c|, plus two roundings
+//                 adding them up (<= 2^-23 |x||c|)
 //   score:        s = fma(-2, dot, cn): 2 * dot error + rounding of cn and of
 //                 the fma, <= 2u (|c|^2 + 2|x||c|)
-// so B = (6D + 14) 2^-22 r^2 / 4 covers it (|x||c| <= r^2 / 4, |c|^2 + 2|x||c|
+// so B = (D + 7) 2^-23 r^2 covers it (|x||c| <= r^2 / 4, |c|^2 + 2|x||c|
 // <= r^2); with the reference's own rounding rho = (D + 4) u (see
 // label_rows_screened), m2 - m1 > T = 2B + 2 rho r^2 proves the label.  T is
-// taken as ((3D + 7) 2^-21 + (2D + 8) 2^-24) r^2 (1.001) + 2^-117 (r + 1);
+// taken as ((D + 8) 2^-22 + (2D + 8) 2^-24) r^2 (1.001) + 2^-117 (r + 1);
 // the last term covers tensor-core inputs and partial sums flushed from the
 // subnormal range (at most 2^-126 per product operand and per step).
 //
@@ -346,7 +352,7 @@ __device__ __forceinline__ void mma_label8(const float* __restrict__ P, uint64_t
     // |x|^2 of points 2t and 2t + 1 from their lanes
     const float nxa = __shfl_sync(0xffffffffu, nx, (2 * t) * 4);
     const float nxb = __shfl_sync(0xffffffffu, nx, (2 * t + 1) * 4);
-    constexpr float A = ((float)(3 * D + 7) * 0x1p-21f + (float)(2 * D + 8) * 0x1p-24f) * 1.001f;
+    constexpr float A = ((float)(D + 8) * 0x1p-22f + (float)(2 * D + 8) * 0x1p-24f) * 1.001f;
     const float ra = (sqrtf(nxa) * (1.0f + 0x1p-16f) + cm) * (1.0f + 0x1p-20f);
     const float rb = (sqrtf(nxb) * (1.0f + 0x1p-16f) + cm) * (1.0f + 0x1p-20f);
     const float Ta = fmaf(A * ra, ra, 0x1p-117f * (ra + 1.0f));
