@@ -143,10 +143,14 @@ __device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t
     }
 }
 
-// d = 32 / 64 jobs with at least MMA_MIN_K clusters: 8 points per warp
-// through the tensor-core screen (mma_label8), then each lane adds its
-// quarter of its point's features into the table.
-constexpr uint32_t MMA_MIN_K = 16;
+// d = 32 / 64 jobs with enough clusters: 8 points per warp through the
+// tensor-core screen (mma_label8), then each lane adds its quarter of its
+// point's features into the table.  Below the thresholds the per-8-point
+// overhead outweighs the MMAs and the FP32 screen is faster (one step of the
+// batched mixture's d = 32 jobs with k in [16, 32) / [32, 64): 0.91 / 1.53 ms
+// on the FP32 screen against 1.33 / 1.75 ms on the tensor cores; d = 64,
+// k in [16, 32) / [32, 64): 2.10 / 3.15 ms against 2.36 / 2.72 ms).
+__host__ __device__ __forceinline__ uint32_t mma_min_k(uint32_t d) { return d == 64 ? 32u : 64u; }
 
 // Shared bytes of the MMA centroid fragments plus |c|^2 (16-byte multiple).
 __host__ __device__ __forceinline__ size_t mma_cent_bytes(uint32_t k, uint32_t d) {
@@ -293,7 +297,7 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
         // the SIMT screen / exact loop, or none) at the start, the sum table
         // in the rest
         const size_t total = cent_cap + acc_cap;
-        const bool mma = (d == 32 || d == 64) && k >= MMA_MIN_K &&
+        const bool mma = (d == 32 || d == 64) && k >= mma_min_k(d) &&
                          mma_cent_bytes(k, d) + ((size_t)k * d + k) * sizeof(float) <= total;
         const size_t cbytes = ((size_t)k * d + ((k + 3u) & ~3u)) * sizeof(float);  // rows + |c|^2
         const bool cent_smem = !mma && cbytes <= cent_cap;

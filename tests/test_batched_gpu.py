@@ -154,7 +154,9 @@ def test_batch_screened_labels_ties_and_nan(ckm, oracle, cuda):
     centroid (an empty cluster: never chosen) in jobs of d = 8..64: labels
     must stay the oracle's."""
     import torch
-    shapes = [(6000, 8, 24), (5000, 32, 40), (3000, 64, 17), (4000, 16, 64)]
+    # SIMT screen: d = 8, 16, (32, k < 64), (64, k < 32); tensor-core screen:
+    # (32, k >= 64), (64, k >= 32)
+    shapes = [(6000, 8, 24), (5000, 32, 40), (3000, 64, 17), (4000, 16, 64), (4000, 64, 40), (3000, 32, 70)]
     jobs, host = make_jobs(cuda, oracle, shapes, seed=11)
     for j in jobs:
         d, k = j["d"], j["k"]
@@ -186,14 +188,16 @@ def test_batch_screened_labels_ties_and_nan(ckm, oracle, cuda):
 
 
 def test_batch_screen_fallback_offsets_and_huge_centroids(ckm, oracle, cuda):
-    """Jobs of d = 8..64 (SIMT screen for k < 16, tensor-core screen for
-    d = 32 / 64 with k >= 16) whose points sit far from the origin (many
-    points fall back from the screen to the exact loop) or that hold a huge or
-    an infinite centroid (every point falls back): labels stay the oracle's."""
+    """Jobs of d = 8..64 (FP32 screen; tensor-core screen for d = 32 with
+    k >= 64 and d = 64 with k >= 32) whose points sit far from the origin
+    (many points fall back from the screen to the exact loop) or that hold a
+    huge or an infinite centroid (every point falls back): labels stay the
+    oracle's."""
     import torch
     # (n, d, k, change)
     cases = [(5000, 8, 20, "offset"), (4000, 64, 24, "offset"), (6000, 32, 30, "offset"), (3000, 64, 9, "huge"),
-             (3000, 64, 40, "inf"), (2000, 32, 5, "-huge"), (2500, 64, 33, "huge"), (2600, 32, 48, "inf")]
+             (3000, 64, 40, "inf"), (2000, 32, 5, "-huge"), (2500, 64, 33, "huge"), (2600, 32, 48, "inf"),
+             (4000, 64, 48, "offset"), (5000, 32, 80, "offset"), (2600, 32, 72, "inf"), (2200, 32, 66, "huge")]
     jobs, host = make_jobs(cuda, oracle, [c[:3] for c in cases], seed=13)
     for i, (j, (n, d, k, change)) in enumerate(zip(jobs, cases)):
         if change == "offset":
