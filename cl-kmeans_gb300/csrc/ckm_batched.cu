@@ -143,21 +143,9 @@ __device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t
     }
 }
 
-// d = 32 / 64 jobs with enough clusters: 8 points per warp through the
-// tensor-core screen (mma_label8), then each lane adds its quarter of its
-// point's features into the table.  Below the thresholds the per-8-point
-// overhead outweighs the MMAs and the FP32 screen is faster (one step of the
-// batched mixture's d = 32 jobs with k in [16, 32) / [32, 64): 0.91 / 1.53 ms
-// on the FP32 screen against 1.33 / 1.75 ms on the tensor cores; d = 64,
-// k in [16, 32) / [32, 64): 2.10 / 3.15 ms against 2.36 / 2.72 ms).
-__host__ __device__ __forceinline__ uint32_t mma_min_k(uint32_t d) { return d == 64 ? 32u : 64u; }
-
-// Shared bytes of the MMA centroid fragments plus |c|^2 (16-byte multiple).
-__host__ __device__ __forceinline__ size_t mma_cent_bytes(uint32_t k, uint32_t d) {
-    const size_t k_pad = mma_k_pad(k);
-    return ((k_pad * d * 2 + k_pad) * sizeof(float) + 15) & ~size_t(15);
-}
-
+// d = 32 / 64 jobs with enough clusters (mma_min_k): 8 points per warp
+// through the tensor-core screen (mma_label8), then each lane adds its
+// quarter of its point's features into the table.
 template <int D, int BT>
 __device__ __forceinline__ void run_tiles_mma(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile,
                                               const float4* frag, const float* s_cn, float cm, float* s_sum,
@@ -279,8 +267,11 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
     __shared__ unsigned int s_last, s_unit, s_cn_max;
     for (;;) {
         // dynamic schedule: the next unclaimed segment (largest first)
-        __syncthreads();  // every thread has read the previous s_unit
-        if (threadIdx.x == 0) s_unit = atomicAdd(work, 1u);
+        __syncthreads();  // every thread has read the previous s_unit and cm
+        if (threadIdx.x == 0) {
+            s_unit = atomicAdd(work, 1u);
+            s_cn_max = 0u;  // zeroed a barrier before any atomicMax of this segment
+        }
         __syncthreads();
         const uint32_t si = s_unit;
         if (si >= num_segs) break;
@@ -308,7 +299,6 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
         float* s_sum = reinterpret_cast<float*>(smem + table_off);
         unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d * copies);
         __syncthreads();  // previous segment's readers of the shared tables are done
-        if (threadIdx.x == 0) s_cn_max = 0u;
         if (mma) {
             if (d == 32) mma_stage_centroids<32>(cent_of(J, parity), k, reinterpret_cast<float4*>(s_c), s_cn, &s_cn_max, threadIdx.x, BT);
             else mma_stage_centroids<64>(cent_of(J, parity), k, reinterpret_cast<float4*>(s_c), s_cn, &s_cn_max, threadIdx.x, BT);

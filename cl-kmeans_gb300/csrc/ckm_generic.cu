@@ -9,6 +9,7 @@
 // global atomics.  Like the low-d kernel, the last CTA finalises.
 #include "ckm_device.cuh"
 #include "ckm_internal.h"
+#include "ckm_mma_screen.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -168,17 +169,22 @@ int launch_generic_t(const GenericArgs<T, L, M>& a, Pass pass, cudaStream_t s) {
 // cluster chains, 128-bit row loads) and adds the registers into the CTA's
 // shared-memory table, merged once into the FP64 scratch.  The generic kernel
 // re-reads the point for every cluster and runs one dependent fma chain at a
-// time; the outputs are the same.  Labels come from the certified screen
-// (label_rows_screened), which falls back to the exact loop per point.
+// time; the outputs are the same.  Labels come from a certified screen, the
+// tensor-core one (mma_label8) for d = 32 with k >= 64 and d = 64 with
+// k >= 32 where its TF32 fragments fit in shared memory, else the FP32 one
+// (label_rows_screened); both fall back to exact arithmetic per point.
 // ---------------------------------------------------------------------------
 
+// label_mode: 0 exact loop, 1 FP32 screen (label_rows_screened), 2 tensor-core
+// screen (mma_label8: 8 points per warp; centroids staged as TF32 fragments).
 template <int D, Pass PASS, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
-    rows_kernel(const GenericArgs<float, uint32_t, uint32_t> a, const uint32_t copies, const int screen) {
+    rows_kernel(const GenericArgs<float, uint32_t, uint32_t> a, const uint32_t copies, const int label_mode) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t k = a.k;
     const uint64_t n = a.n;
     const uint32_t kd = k * D;
+    const bool mma = label_mode == 2;
     // `copies` (a power of two up to 32) interleaved copies of the sums,
     // s_sum[(f * k + c) * copies + (lane & (copies - 1))]: a shared-memory
     // FP32 atomic add retries while other lanes of the warp hit the same word,
@@ -186,37 +192,69 @@ __global__ void __launch_bounds__(NT, MINB)
     // (integer atomics, which do not slow down that way) keep one copy.
     const uint32_t lane_off = threadIdx.x & (copies - 1u);
     __shared__ unsigned int s_cn_max;
-    float* s_c = reinterpret_cast<float*>(smem);  // [c * D + f]
-    float* s_cn = s_c + kd;                        // |c|^2 for the screen
-    float* s_sum = s_cn + ((k + 3u) & ~3u);
+    float* s_c = reinterpret_cast<float*>(smem);  // rows [c * D + f], or the MMA fragments
+    float* s_cn = mma ? s_c + (size_t)mma_k_pad(k) * D * 2 : s_c + kd;  // |c|^2 for the screens
+    float* s_sum = mma ? reinterpret_cast<float*>(smem + mma_cent_bytes(k, D)) : s_cn + ((k + 3u) & ~3u);
     unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)kd * copies);
 
     if (threadIdx.x == 0) s_cn_max = 0u;
-    for (uint32_t i = threadIdx.x; i < kd; i += NT) {
-        const uint32_t c = i / D, f = i - c * D;
-        s_c[i] = a.centroids[(size_t)f * k + c];
-    }
     if constexpr (PASS == Pass::Fused) {
         const size_t words = (size_t)kd * copies + k;
         for (size_t i = threadIdx.x; i < words; i += NT) s_sum[i] = 0.0f;  // sums, then masses
     }
-    __syncthreads();
-    if (screen) {
-        screen_norms(s_c, D, k, s_cn, &s_cn_max, threadIdx.x, NT);
+    if (mma) {
+        __syncthreads();  // s_cn_max is zero before the staging's atomicMax
+        mma_stage_centroids<D>(a.centroids, k, reinterpret_cast<float4*>(s_c), s_cn, &s_cn_max, threadIdx.x, NT);
         __syncthreads();
+    } else {
+        for (uint32_t i = threadIdx.x; i < kd; i += NT) {
+            const uint32_t c = i / D, f = i - c * D;
+            s_c[i] = a.centroids[(size_t)f * k + c];
+        }
+        __syncthreads();
+        if (label_mode == 1) {
+            screen_norms(s_c, D, k, s_cn, &s_cn_max, threadIdx.x, NT);
+            __syncthreads();
+        }
     }
     const float cm = screen_cm(s_cn_max);
 
-    for (uint64_t p = (uint64_t)blockIdx.x * NT + threadIdx.x; p < n; p += (uint64_t)gridDim.x * NT) {
-        float x[D];
+    if (mma) {
+        // 8 points per warp iteration; each lane adds its quarter of its
+        // point's features (x = hi + mid exactly)
+        const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3u;
+        const uint64_t stride = (uint64_t)gridDim.x * (NT / 32) * 8;
+#pragma unroll 1
+        for (uint64_t p0 = ((uint64_t)blockIdx.x * (NT / 32) + warp) * 8; p0 < n; p0 += stride) {
+            uint32_t bh[D / 4], bm[D / 4];
+            uint32_t lab;
+            mma_label8<D>(a.points, n, p0, n, reinterpret_cast<const float4*>(s_c), s_cn, cm, k, bh, bm, lab);
+            if (p0 + g < n) {
+                if (t == 0) a.labels[p0 + g] = lab;
+                if constexpr (PASS == Pass::Fused) {
 #pragma unroll
-        for (int f = 0; f < D; ++f) x[f] = __ldg(a.points + (uint64_t)f * n + p);
-        const uint32_t lab = screen ? label_rows_screened<D>(x, s_c, s_cn, cm, k) : label_rows_exact<D>(x, s_c, k);
-        a.labels[p] = lab;
-        if constexpr (PASS == Pass::Fused) {
+                    for (uint32_t i = 0; i < (uint32_t)D / 4; ++i) {
+                        const uint32_t f = (i >> 1) * 8 + t + ((i & 1u) ? 4u : 0u);
+                        atomicAdd(&s_sum[((size_t)f * k + lab) * copies + lane_off],
+                                  __uint_as_float(bh[i]) + __uint_as_float(bm[i]));
+                    }
+                    if (t == 0) atomicAdd(&s_mass[lab], 1u);
+                }
+            }
+        }
+    } else {
+        for (uint64_t p = (uint64_t)blockIdx.x * NT + threadIdx.x; p < n; p += (uint64_t)gridDim.x * NT) {
+            float x[D];
 #pragma unroll
-            for (int f = 0; f < D; ++f) atomicAdd(&s_sum[((size_t)f * k + lab) * copies + lane_off], x[f]);
-            atomicAdd(&s_mass[lab], 1u);
+            for (int f = 0; f < D; ++f) x[f] = __ldg(a.points + (uint64_t)f * n + p);
+            const uint32_t lab =
+                label_mode == 1 ? label_rows_screened<D>(x, s_c, s_cn, cm, k) : label_rows_exact<D>(x, s_c, k);
+            a.labels[p] = lab;
+            if constexpr (PASS == Pass::Fused) {
+#pragma unroll
+                for (int f = 0; f < D; ++f) atomicAdd(&s_sum[((size_t)f * k + lab) * copies + lane_off], x[f]);
+                atomicAdd(&s_mass[lab], 1u);
+            }
         }
     }
 
@@ -244,18 +282,20 @@ __global__ void __launch_bounds__(NT, MINB)
     }
 }
 
-size_t rows_smem_bytes(uint32_t d, uint32_t k, Pass pass, uint32_t copies) {
+size_t rows_smem_bytes(uint32_t d, uint32_t k, Pass pass, uint32_t copies, bool mma) {
     const size_t kd = (size_t)k * d;
-    const size_t cent = kd + ((k + 3) & ~size_t(3));  // rows + |c|^2
-    return (pass == Pass::Fused ? cent + kd * copies + k : cent) * sizeof(float);
+    const size_t cent = mma ? mma_cent_bytes(k, d) : (kd + ((k + 3) & ~size_t(3))) * sizeof(float);  // + |c|^2
+    return cent + (pass == Pass::Fused ? (kd * copies + k) * sizeof(float) : 0);
 }
 
-// The certified screen (label_rows_screened) is on unless the environment
-// variable CKM_SCREEN is "0" (exact arithmetic for every cluster).
-int screen_enabled() {
+// The labelling of the rows kernel: the environment variable CKM_SCREEN = "0"
+// selects the exact loop for every cluster, "1" the FP32 screen for every
+// shape; otherwise the tensor-core screen where mma_min_k allows, else the
+// FP32 screen.
+int screen_setting() {
     static int v = [] {
         const char* e = getenv("CKM_SCREEN");
-        return (e && e[0] == '0') ? 0 : 1;
+        return (e && (e[0] == '0' || e[0] == '1')) ? e[0] - '0' : 2;
     }();
     return v;
 }
@@ -264,7 +304,8 @@ constexpr size_t ROWS_TWO_CTA_LIMIT = 110 * 1024;  // two 256-thread CTAs per SM
 constexpr size_t ROWS_COPIES_LIMIT = 200 * 1024;  // tables of several copies up to this size
 
 template <int D, Pass PASS, int NT, int MINB>
-int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, uint32_t copies, cudaStream_t s) {
+int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, uint32_t copies, int label_mode,
+                  cudaStream_t s) {
     auto kern = rows_kernel<D, PASS, NT, MINB>;
     static std::mutex mu;
     static bool attr_done[64] = {false};
@@ -287,10 +328,11 @@ int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, 
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, NT, smem);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy(rows)");
     if (bps < 1) return fail(CKM_ERR_UNSUPPORTED, "rows: kernel does not fit on an SM");
-    const uint64_t blocks = (a.n + NT - 1) / NT;
+    const uint64_t per_cta = label_mode == 2 ? (uint64_t)(NT / 32) * 8 : (uint64_t)NT;
+    const uint64_t blocks = (a.n + per_cta - 1) / per_cta;
     uint64_t grid = std::min<uint64_t>(blocks, (uint64_t)di.sm_count * bps);
     if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, NT, smem, s>>>(a, copies, screen_enabled());
+    kern<<<(unsigned)grid, NT, smem, s>>>(a, copies, label_mode);
     count_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "rows launch");
@@ -298,23 +340,27 @@ int launch_rows_v(const GenericArgs<float, uint32_t, uint32_t>& a, size_t smem, 
 
 template <int D, Pass PASS>
 int launch_rows_d(const GenericArgs<float, uint32_t, uint32_t>& a, cudaStream_t s) {
+    const int setting = screen_setting();
+    bool mma = setting == 2 && a.k >= mma_min_k(D) &&
+               rows_smem_bytes(D, a.k, PASS, 1, true) + 1024 <= device_info().smem_optin;
+    const int label_mode = mma ? 2 : (setting == 0 ? 0 : 1);
     // the most copies that keep the table within the limit (one at least)
     uint32_t copies = 1;
     if (PASS == Pass::Fused)
         for (uint32_t c = 32; c > 1; c >>= 1)
-            if (rows_smem_bytes(D, a.k, PASS, c) <= ROWS_COPIES_LIMIT) {
+            if (rows_smem_bytes(D, a.k, PASS, c, mma) <= ROWS_COPIES_LIMIT) {
                 copies = c;
                 break;
             }
-    const size_t smem = rows_smem_bytes(D, a.k, PASS, copies);
-    if (smem <= ROWS_TWO_CTA_LIMIT) return launch_rows_v<D, PASS, 256, 2>(a, smem, copies, s);
-    return launch_rows_v<D, PASS, 512, 1>(a, smem, copies, s);
+    const size_t smem = rows_smem_bytes(D, a.k, PASS, copies, mma);
+    if (smem <= ROWS_TWO_CTA_LIMIT) return launch_rows_v<D, PASS, 256, 2>(a, smem, copies, label_mode, s);
+    return launch_rows_v<D, PASS, 512, 1>(a, smem, copies, label_mode, s);
 }
 
 // Returns -1000 when the shape is not one the rows kernel takes.
 int try_launch_rows(const GenericArgs<float, uint32_t, uint32_t>& a, Pass pass, cudaStream_t s) {
     if (pass == Pass::SumsOnly || (a.d != 32 && a.d != 64)) return -1000;
-    if (rows_smem_bytes(a.d, a.k, pass, 1) + 1024 > device_info().smem_optin) return -1000;
+    if (rows_smem_bytes(a.d, a.k, pass, 1, false) + 1024 > device_info().smem_optin) return -1000;
     if (pass == Pass::Fused) return a.d == 32 ? launch_rows_d<32, Pass::Fused>(a, s) : launch_rows_d<64, Pass::Fused>(a, s);
     return a.d == 32 ? launch_rows_d<32, Pass::LabelOnly>(a, s) : launch_rows_d<64, Pass::LabelOnly>(a, s);
 }

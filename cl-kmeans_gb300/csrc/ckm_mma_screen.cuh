@@ -71,6 +71,19 @@ __device__ __forceinline__ size_t mma_frag_index(uint32_t mt, uint32_t ks, uint3
 
 __host__ __device__ __forceinline__ uint32_t mma_k_pad(uint32_t k) { return (k + 15u) & ~15u; }
 
+// Shared bytes of the MMA centroid fragments plus |c|^2 (16-byte multiple).
+__host__ __device__ __forceinline__ size_t mma_cent_bytes(uint32_t k, uint32_t d) {
+    const size_t k_pad = mma_k_pad(k);
+    return ((k_pad * d * 2 + k_pad) * sizeof(float) + 15) & ~size_t(15);
+}
+
+// Smallest k that takes the tensor-core screen.  Below it the per-8-point
+// overhead outweighs the MMAs and the FP32 screen is faster (one step of the
+// batched mixture's d = 32 jobs with k in [16, 32) / [32, 64): 0.91 / 1.53 ms
+// on the FP32 screen against 1.33 / 1.75 ms on the tensor cores; d = 64,
+// k in [16, 32) / [32, 64): 2.10 / 3.15 ms against 2.36 / 2.72 ms).
+__host__ __device__ __forceinline__ uint32_t mma_min_k(uint32_t d) { return d == 64 ? 32u : 64u; }
+
 // Stages the column-major centroids C[f * k + c] into that layout and
 // cn[c] = |c|^2 (FP64 sum, one rounding; NaN for padding), and the maximum of
 // the non-NaN cn into *s_cn_max (zeroed by the caller).  All threads of the

@@ -78,6 +78,12 @@ SHAPES = [
     (7000, 32, 600),
     (3000, 64, 1),
     (4100, 32, 2),
+    # rows kernel on the tensor-core screen (d = 32 with k >= 64, d = 64 with
+    # k >= 32, while the TF32 fragments fit in shared memory)
+    (9000, 64, 40),
+    (8000, 32, 100),
+    (5000, 64, 200),
+    (3001, 32, 64),
 ]
 
 
@@ -93,7 +99,8 @@ def test_fused_one_iteration_matches_oracle(ckm, oracle, cuda, n, d, k):
 
 
 @pytest.mark.parametrize("n,d,k,iters", [(1 << 16, 4, 16, 20), (40000, 2, 10, 15), (30001, 8, 24, 10),
-                                         (20000, 20, 12, 8), (16384, 64, 40, 6), (12000, 32, 13, 6)])
+                                         (20000, 20, 12, 8), (16384, 64, 40, 6), (12000, 32, 13, 6),
+                                         (12000, 32, 90, 5)])
 def test_fused_lockstep_iterations(ckm, oracle, cuda, n, d, k, iters):
     import torch
     P = blobs(n, d, k, seed=7 * n + d)
@@ -134,7 +141,7 @@ def test_ties_pick_lowest_index_and_nan_never_wins(ckm, oracle, cuda):
     assert not np.any(np.isin(labels2, [3, 5]))
 
 
-@pytest.mark.parametrize("d,k", [(32, 9), (64, 6), (64, 260)])
+@pytest.mark.parametrize("d,k", [(32, 9), (64, 6), (64, 260), (64, 40), (32, 70)])
 def test_rows_kernel_ties_nan_and_labeling(ckm, oracle, cuda, d, k):
     """d = 32 / 64 (fixed-d rows kernel): exact ties inside and across the
     four-cluster steps pick the lowest index, a NaN centroid never wins, and
@@ -159,14 +166,16 @@ def test_rows_kernel_ties_nan_and_labeling(ckm, oracle, cuda, d, k):
     assert np.array_equal(dL.cpu().numpy().view(np.uint32), ref)
 
 
-@pytest.mark.parametrize("d,case", [(32, "offset"), (64, "offset"), (64, "huge"), (32, "inf")])
-def test_screen_fallback_keeps_reference_labels(ckm, oracle, cuda, d, case):
+@pytest.mark.parametrize("d,case,k", [(32, "offset", 24), (64, "offset", 24), (64, "huge", 24), (32, "inf", 24),
+                                      (64, "offset", 48), (32, "offset", 80), (64, "huge", 40), (32, "inf", 72)])
+def test_screen_fallback_keeps_reference_labels(ckm, oracle, cuda, d, case, k):
     """d = 32 / 64 label through the certified screen.  Points it cannot prove
     are labelled with the exact loop: data far from the origin (the rounding
     bound grows with |x| + max|c|, so many points fall back), a centroid so
     large that (|x| + max|c|)^2 >= 2^120 (every point falls back), and an
-    infinite centroid (every point falls back; that cluster never wins)."""
-    n, k = 6000, 24
+    infinite centroid (every point falls back; that cluster never wins).
+    k = 24: FP32 screen; k = 40..80: tensor-core screen."""
+    n = 6000
     P = blobs(n, d, 8, seed=d + len(case))
     if case == "offset":
         P = (P + np.float32(3000.0)).astype(np.float32)
