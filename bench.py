@@ -68,14 +68,14 @@ def measured_hbm_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic_per_point(workload):
+def profiled_traffic_per_point(workload, key="dram_bytes_per_point"):
     """DRAM bytes per point-iteration from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "fused_lowd_d4_k16.md")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for line in f:
-            if line.strip().startswith("dram_bytes_per_point:"):
+            if line.strip().startswith(key + ":"):
                 try:
                     return float(line.split(":", 1)[1].strip())
                 except ValueError:
@@ -718,6 +718,8 @@ def main():
     ap.add_argument("--no-simt-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-spatial", action="store_true",
+                    help="default workload: time the caller's point order only (no spatial sort, no box pruning)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     workload = args.workload
@@ -763,6 +765,33 @@ def main():
     def step(i):
         ckm.fused(P, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stream)
 
+    def timed(step_fn, it0):
+        """K steps bracketed by a barrier + synchronize, CUDA events on the
+        launching stream around the whole region and around every launch."""
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        launches0 = ckm.launch_count()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            step_fn(it0 + i)
+            evs[i][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        launches = ckm.launch_count() - launches0
+        total_ms = t_start.elapsed_time(t_end)
+        per_launch_ms = [a_.elapsed_time(b_) for a_, b_ in evs]
+        if world > 1:
+            t = torch.tensor([total_ms], dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(t.item())
+        return total_ms, per_launch_ms, launches
+
     for i in range(args.warmup):
         step(i)
     torch.cuda.synchronize()
@@ -770,40 +799,48 @@ def main():
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    launches0 = ckm.launch_count()
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    for i in range(args.steps):
-        evs[i][0].record(stream)
-        step(args.warmup + i)
-        evs[i][1].record(stream)
-    t_end.record(stream)
-    torch.cuda.synchronize()
-    gpu_launches = ckm.launch_count() - launches0
+    # the caller's point order
+    u_total_ms, u_per_launch, u_launches = timed(step, args.warmup)
+    it_next = args.warmup + args.steps
+    spatial = None
+    if not args.no_spatial:
+        # the same points in spatial (Z-) order, prepared once outside the
+        # timed steps (ckm_spatial_sort_f32); the pruned kernel's labels are
+        # the reference's on these points, and perm maps them back
+        torch.cuda.synchronize()
+        ts0 = time.perf_counter()
+        Ps, perm = ckm.spatial_sort(P, n, d, stream)
+        torch.cuda.synchronize()
+        prepare_ms = (time.perf_counter() - ts0) * 1e3
+
+        def step_sorted(i):
+            ckm.fused_sorted(Ps, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stream)
+
+        for i in range(args.warmup):
+            step_sorted(it_next + i)
+        it_next += args.warmup
+        total_ms, per_launch_ms, gpu_launches = timed(step_sorted, it_next)
+        spatial = {"prepare_ms": prepare_ms, "call": "ckm_spatial_sort_f32 once, then ckm_fused_sorted_f32 per step"}
+    else:
+        total_ms, per_launch_ms, gpu_launches = u_total_ms, u_per_launch, u_launches
     clocks = sampler.stop()
-    total_ms = t_start.elapsed_time(t_end)
-    per_launch_ms = [a.elapsed_time(b) for a, b in evs]
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
     value = n * args.steps * world / (total_ms / 1e3)
     avg_launch_s = statistics.mean(per_launch_ms) / 1e3
+    unsorted = {"value": n * args.steps * world / (u_total_ms / 1e3), "ms_per_step": u_total_ms / args.steps,
+                "call": "ckm_fused_f32 on the points in generation order"}
 
     # --- roofline of the fused kernel --------------------------------------
     bytes_per_point = 4 * d + 4
     achieved = bytes_per_point * n / avg_launch_s / 1e9
     peak, peak_kind = measured_hbm_peak()
-    tpp = profiled_traffic_per_point(workload)
+    tpp = profiled_traffic_per_point(workload, "dram_bytes_per_point" if args.no_spatial
+                                     else "dram_bytes_per_point_spatial")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind,
                 "traffic": (tpp * n) if tpp is not None else None,
                 "algorithmic_bytes_per_launch": bytes_per_point * n}
+    u_achieved = bytes_per_point * n / (statistics.mean(u_per_launch) / 1e3) / 1e9
+    unsorted["roofline_frac"] = u_achieved / peak
 
     # --- e2e through the C ABI with pinned host buffers --------------------
     e2e = None
@@ -852,11 +889,13 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian mixture generated on the device)",
             "config": {"workload": workload, "n": n, "d": d, "k": k, "blobs": blobs, "sigma": [slo, shi],
-                       "seed": SEED, "init": "first_x", "layout": "column-major",
+                       "seed": SEED, "init": "first_x",
+                       "layout": "column-major" + ("" if args.no_spatial else
+                                                  ", points in spatial order (sorted once before the timed steps)"),
                        "l2": "inputs (%.1f GiB) larger than L2, no flush" % (n * (d + 1) * 4 / 2 ** 30),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(gpu_launches),
-            "clocks": clocks,
+            "clocks": clocks, "spatial_order": spatial, "caller_order": unsorted,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

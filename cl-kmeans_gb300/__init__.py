@@ -37,6 +37,7 @@ EXPORTS = [
     "ckm_matrix_add_u32", "ckm_matrix_add_u64", "ckm_reduce_vector_parcol_u32",
     "ckm_finalize_f32", "ckm_finalize_f64", "ckm_generate_mixture_f32",
     "ckm_kmeans_run_f32", "ckm_kmeans_run_f64",
+    "ckm_spatial_sort_workspace_bytes", "ckm_spatial_sort_f32", "ckm_fused_sorted_f32", "ckm_unpermute_u32",
 ]
 
 
@@ -131,6 +132,10 @@ def lib():
                                 ctypes.POINTER(RunInfo)], i32),
         "ckm_kmeans_run_f64": ([ctypes.POINTER(RunConfig), u32, u32, u64, u32, vp, vp, vp, vp,
                                 ctypes.POINTER(RunInfo)], i32),
+        "ckm_spatial_sort_workspace_bytes": ([], sz),
+        "ckm_spatial_sort_f32": ([u32, u64, vp, vp, vp, vp, sz, vp], i32),
+        "ckm_fused_sorted_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
+        "ckm_unpermute_u32": ([u64, vp, vp, vp, vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -183,6 +188,33 @@ def fused(points, old_centroids, new_centroids, labels, masses, scratch, n, d, k
     fn = lib().ckm_fused_f64 if _is64(points) else lib().ckm_fused_f32
     check(fn(d, n, k, _p(points), _p(old_centroids), _p(new_centroids), _p(labels), _p(masses), _p(scratch),
              scratch.numel(), mode, _stream(stream)), "ckm_fused")
+
+
+def spatial_sort(points, n, d, stream=None):
+    """ckm_spatial_sort_f32: (sorted column-major points, perm) on the points'
+    device; perm[q] is the index in `points` of sorted point q."""
+    import torch
+    L = lib()
+    out = torch.empty_like(points)
+    perm = torch.empty(n, dtype=torch.int32, device=points.device)
+    ws = torch.empty(int(L.ckm_spatial_sort_workspace_bytes()), dtype=torch.uint8, device=points.device)
+    check(L.ckm_spatial_sort_f32(d, n, _p(points), _p(out), _p(perm), _p(ws), ws.numel(), _stream(stream)),
+          "ckm_spatial_sort_f32")
+    return out, perm
+
+
+def fused_sorted(points, old_centroids, new_centroids, labels, masses, scratch, n, d, k, mode=MODE_FINALIZE,
+                 stream=None):
+    """ckm_fused_sorted_f32: ckm_fused_f32 with per-warp box pruning (for
+    spatially ordered points); labels in the order of `points`."""
+    check(lib().ckm_fused_sorted_f32(d, n, k, _p(points), _p(old_centroids), _p(new_centroids), _p(labels),
+                                     _p(masses), _p(scratch), scratch.numel(), mode, _stream(stream)),
+          "ckm_fused_sorted_f32")
+
+
+def unpermute(perm, labels_in, labels_out, n, stream=None):
+    """ckm_unpermute_u32: labels_out[perm[q]] = labels_in[q]."""
+    check(lib().ckm_unpermute_u32(n, _p(perm), _p(labels_in), _p(labels_out), _stream(stream)), "ckm_unpermute_u32")
 
 
 def fused_noalloc(points, old_centroids, new_centroids, labels, masses, n, d, k, mode=MODE_FINALIZE,

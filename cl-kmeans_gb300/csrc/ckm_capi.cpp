@@ -166,6 +166,46 @@ int ckm_fused_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, const
     return launch_generic_f32(a, Pass::Fused, s);
 }
 
+int ckm_fused_sorted_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, const float* old_centroids,
+                         float* new_centroids, uint32_t* labels, uint32_t* masses, void* scratch,
+                         size_t scratch_bytes, int mode, ckm_stream_t stream) {
+    int st = check_shape(d, n, k);
+    if (st) return st;
+    if (!valid_mode(mode)) return fail(CKM_ERR_INVALID_ARGUMENT, "mode must be DEFER, FINALIZE or ACCUMULATE");
+    if ((st = check_scratch(scratch, scratch_bytes, d, k))) return st;
+    if (n > 0 && (!points || !labels)) return fail(CKM_ERR_INVALID_ARGUMENT, "points/labels NULL");
+    if (!old_centroids) return fail(CKM_ERR_INVALID_ARGUMENT, "old_centroids NULL");
+    if (mode != CKM_MODE_DEFER && (!new_centroids || !masses))
+        return fail(CKM_ERR_INVALID_ARGUMENT, "new_centroids/masses NULL");
+    FusedF32 a{points, old_centroids, labels, new_centroids, masses,
+               scratch_view(scratch, scratch_layout(d, k)), n, d, k, mode};
+    a.flags = FUSED_BOX_PRUNE;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (lowd_supported(d, k)) return launch_fused_f32(a, Pass::Fused, s);
+    return launch_generic_f32(a, Pass::Fused, s);
+}
+
+size_t ckm_spatial_sort_workspace_bytes(void) { return spatial_sort_workspace_bytes(); }
+
+int ckm_spatial_sort_f32(uint32_t d, uint64_t n, const float* points, float* sorted_points, uint32_t* perm,
+                         void* workspace, size_t workspace_bytes, ckm_stream_t stream) {
+    if (d == 0 || d > 16) return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: num_features must be 1..16");
+    if (n > 0xffffffffull) return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: num_points must be < 2^32");
+    if (n > 0 && (!points || !sorted_points || !perm))
+        return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: NULL pointer");
+    if (points == sorted_points && n > 0)
+        return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: sorted_points must not alias points");
+    if (!workspace || workspace_bytes < spatial_sort_workspace_bytes())
+        return fail(CKM_ERR_SCRATCH_TOO_SMALL, "spatial sort: workspace smaller than ckm_spatial_sort_workspace_bytes()");
+    return launch_spatial_sort(d, n, points, sorted_points, perm, workspace, (cudaStream_t)stream);
+}
+
+int ckm_unpermute_u32(uint64_t n, const uint32_t* perm, const uint32_t* in, uint32_t* out, ckm_stream_t stream) {
+    if (n > 0 && (!perm || !in || !out)) return fail(CKM_ERR_INVALID_ARGUMENT, "unpermute: NULL pointer");
+    if (in == out && n > 0) return fail(CKM_ERR_INVALID_ARGUMENT, "unpermute: out must not alias in");
+    return launch_unpermute_u32(n, perm, in, out, (cudaStream_t)stream);
+}
+
 int ckm_fused_f64(uint32_t d, uint64_t n, uint32_t k, const double* points, const double* old_centroids,
                   double* new_centroids, uint64_t* labels, uint64_t* masses, void* scratch, size_t scratch_bytes,
                   int mode, ckm_stream_t stream) {

@@ -62,7 +62,13 @@ struct FusedF32 {
     uint64_t n;
     uint32_t d, k;
     int mode;
+    // FUSED_BOX_PRUNE: per warp, skip the clusters that are provably farther
+    // than another one from every point of the warp (points in spatial order,
+    // e.g. from spatial_sort, make this effective); labels are unchanged.
+    uint32_t flags = 0;
 };
+
+constexpr uint32_t FUSED_BOX_PRUNE = 1u;
 
 struct FusedF64 {
     const double* points;
@@ -80,6 +86,11 @@ enum class Pass { Fused, LabelOnly, SumsOnly };
 
 // Launchers (return CKM_OK or an error status; never throw).
 int launch_fused_f32(const FusedF32& a, Pass pass, cudaStream_t s);
+// Spatial order (ckm_spatial.cu): counting sort by a Z-order cell key.
+size_t spatial_sort_workspace_bytes();
+int launch_spatial_sort(uint32_t d, uint64_t n, const float* points, float* sorted, uint32_t* perm, void* ws,
+                        cudaStream_t s);
+int launch_unpermute_u32(uint64_t n, const uint32_t* perm, const uint32_t* in, uint32_t* out, cudaStream_t s);
 int launch_generic_f32(const FusedF32& a, Pass pass, cudaStream_t s);
 int launch_generic_f64(const FusedF64& a, Pass pass, cudaStream_t s);
 bool lowd_supported(uint32_t d, uint32_t k);

@@ -92,7 +92,104 @@ __device__ __forceinline__ void load_tile(Tile<D, PPT>& T, const FusedF32& a, ui
     }
 }
 
-template <int D, int PPT, int ACC, Pass PASS, int NT>
+// Order-preserving map of floats to unsigned integers (and back), so warp
+// minima / maxima of floats run as one integer reduction.
+__device__ __forceinline__ uint32_t f2o(float x) {
+    const uint32_t b = __float_as_uint(x);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Box pruning (k <= 32): the clusters that can hold the reference's label of
+// some point of this warp.  The warp's points lie in the box [lo, hi]
+// (per-feature minima and maxima; NaN coordinates are left out: a point with
+// a NaN has NaN distances everywhere and label 0 whatever is pruned).  For
+// cluster c, LB_c = sum_f max(lo_f - c_f, c_f - hi_f, 0)^2 (rounded down) is
+// at most its squared distance to any point of the box, UB_c =
+// sum_f max(|c_f - lo_f|, |c_f - hi_f|)^2 (rounded up) at least.  With the
+// reference's FP32 distance within (1 +- rho) of the exact one,
+// rho = (D + 4) 2^-24, a cluster with LB_c (1 - rho) > min UB (1 + rho) +
+// 2^-120 (underflow) is farther, in the reference's arithmetic, than the
+// cluster of min UB from every point of the box: it can neither be the
+// label nor tie it.  The mask is the same in every lane.
+template <int D, int PPT>
+__device__ __forceinline__ uint32_t box_prune_mask(const Tile<D, PPT>& T, uint64_t p0, uint64_t n,
+                                                   const float2* __restrict__ s_c, uint32_t k) {
+    const uint32_t lane = threadIdx.x & 31u;
+    float lo[D], hi[D];
+#pragma unroll
+    for (int f = 0; f < D; ++f) {
+        lo[f] = INFINITY;
+        hi[f] = -INFINITY;
+    }
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+        if (p0 + i < n) {
+#pragma unroll
+            for (int f = 0; f < D; ++f) {
+                lo[f] = fminf(lo[f], T.x[f][i]);
+                hi[f] = fmaxf(hi[f], T.x[f][i]);
+            }
+        }
+#pragma unroll
+    for (int f = 0; f < D; ++f) {
+        lo[f] = o2f(__reduce_min_sync(0xffffffffu, f2o(lo[f])));
+        hi[f] = o2f(__reduce_max_sync(0xffffffffu, f2o(hi[f])));
+    }
+    float lb = INFINITY, ub = INFINITY;
+    if (lane < k) {
+        lb = 0.0f;
+        ub = 0.0f;
+#pragma unroll
+        for (int f = 0; f < D; ++f) {
+            const float c = s_c[lane * D + f].x;
+            const float g = fmaxf(fmaxf(__fsub_rd(lo[f], c), __fsub_rd(c, hi[f])), 0.0f);
+            lb = __fmaf_rd(g, g, lb);
+            const float u = fmaxf(fmaxf(__fsub_ru(c, lo[f]), __fsub_ru(lo[f], c)),
+                                  fmaxf(__fsub_ru(c, hi[f]), __fsub_ru(hi[f], c)));
+            ub = __fmaf_ru(u, u, ub);
+        }
+        if (isnan(ub)) ub = INFINITY;
+    }
+    const float ub_min = o2f(__reduce_min_sync(0xffffffffu, f2o(ub)));
+    constexpr float kLo = 1.0f - (float)(D + 4) * 0x1p-24f;       // exact
+    constexpr float kHi = 1.0f + (float)((D + 5) / 2) * 0x1p-23f;  // exact, >= 1 + (D + 4) 2^-24
+    const bool far = __fmul_rd(lb, kLo) > __fadd_ru(__fmul_ru(ub_min, kHi), 0x1p-120f);
+    return __ballot_sync(0xffffffffu, lane < k && !far);
+}
+
+// One cluster against the thread's PPT points: the reference's distance
+// (t = x_f - c_f, fma(t, t, acc)) two points per packed op, and the strict
+// '<' argmin update.
+template <int D, int PPT>
+__device__ __forceinline__ void dist_argmin(Tile<D, PPT>& T, float (&best)[PPT], const float2* __restrict__ cp,
+                                            uint32_t c) {
+    float2 cc[D];
+#pragma unroll
+    for (int f = 0; f < D; ++f) cc[f] = cp[f];
+#pragma unroll
+    for (int j = 0; j < PPT / 2; ++j) {
+        float2 t = sub2(make_float2(T.x[0][2 * j], T.x[0][2 * j + 1]), cc[0]);
+        float2 acc = mul2(t, t);  // == fma(t, t, 0) exactly
+#pragma unroll
+        for (int f = 1; f < D; ++f) {
+            t = sub2(make_float2(T.x[f][2 * j], T.x[f][2 * j + 1]), cc[f]);
+            acc = fma2(t, t, acc);
+        }
+        if (acc.x < best[2 * j]) {
+            best[2 * j] = acc.x;
+            T.lab[2 * j] = c;
+        }
+        if (acc.y < best[2 * j + 1]) {
+            best[2 * j + 1] = acc.y;
+            T.lab[2 * j + 1] = c;
+        }
+    }
+}
+
+template <int D, int PPT, int ACC, Pass PASS, int NT, bool PRUNE>
 __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a, uint64_t p0, bool vec,
                                              const float2* __restrict__ s_c, float* __restrict__ s_acc) {
     constexpr int VW = LowdCfg<D>::VW;
@@ -106,30 +203,19 @@ __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a,
             best[i] = FLT_MAX;
             T.lab[i] = 0u;
         }
-        const float2* cp = s_c;
-#pragma unroll 2
-        for (uint32_t c = 0; c < k; ++c, cp += D) {
-            float2 cc[D];
-#pragma unroll
-            for (int f = 0; f < D; ++f) cc[f] = cp[f];
-#pragma unroll
-            for (int j = 0; j < PPT / 2; ++j) {
-                float2 t = sub2(make_float2(T.x[0][2 * j], T.x[0][2 * j + 1]), cc[0]);
-                float2 acc = mul2(t, t);  // == fma(t, t, 0) exactly
-#pragma unroll
-                for (int f = 1; f < D; ++f) {
-                    t = sub2(make_float2(T.x[f][2 * j], T.x[f][2 * j + 1]), cc[f]);
-                    acc = fma2(t, t, acc);
-                }
-                if (acc.x < best[2 * j]) {
-                    best[2 * j] = acc.x;
-                    T.lab[2 * j] = c;
-                }
-                if (acc.y < best[2 * j + 1]) {
-                    best[2 * j + 1] = acc.y;
-                    T.lab[2 * j + 1] = c;
-                }
+        if constexpr (PRUNE) {
+            // the surviving clusters in ascending order: the same strict '<'
+            // scan as below over a subset that holds every point's label
+            uint32_t m = box_prune_mask<D, PPT>(T, p0, n, s_c, k);
+            while (m) {
+                const uint32_t c = __ffs(m) - 1;
+                m &= m - 1;
+                dist_argmin<D, PPT>(T, best, s_c + c * D, c);
             }
+        } else {
+            const float2* cp = s_c;
+#pragma unroll 2
+            for (uint32_t c = 0; c < k; ++c, cp += D) dist_argmin<D, PPT>(T, best, cp, c);
         }
         // labels out
         if (vec && p0 + PPT <= n) {
@@ -217,7 +303,7 @@ __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a,
     }
 }
 
-template <int D, int PPT, int ACC, Pass PASS, int NT, int MINB, bool PREF>
+template <int D, int PPT, int ACC, Pass PASS, int NT, int MINB, bool PREF, bool PRUNE = false>
 __global__ void __launch_bounds__(NT, MINB)
     lowd_kernel(const FusedF32 a, const int vec_ok, const uint64_t ntiles) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -250,18 +336,18 @@ __global__ void __launch_bounds__(NT, MINB)
         while (t < ntiles) {
             const uint64_t t1 = t + gridDim.x;
             if (t1 < ntiles) load_tile<D, PPT, PASS>(B, a, t1 * TILE + threadIdx.x * PPT, vec);
-            process_tile<D, PPT, ACC, PASS, NT>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
+            process_tile<D, PPT, ACC, PASS, NT, PRUNE>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
             if (t1 >= ntiles) break;
             const uint64_t t2 = t1 + gridDim.x;
             if (t2 < ntiles) load_tile<D, PPT, PASS>(A, a, t2 * TILE + threadIdx.x * PPT, vec);
-            process_tile<D, PPT, ACC, PASS, NT>(B, a, t1 * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
+            process_tile<D, PPT, ACC, PASS, NT, PRUNE>(B, a, t1 * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
             t = t2;
         }
     } else {
         for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
             Tile<D, PPT> A;
             load_tile<D, PPT, PASS>(A, a, t * TILE + threadIdx.x * PPT, vec);
-            process_tile<D, PPT, ACC, PASS, NT>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
+            process_tile<D, PPT, ACC, PASS, NT, PRUNE>(A, a, t * TILE + threadIdx.x * PPT, vec, s_c, s_acc);
         }
     }
 
@@ -340,10 +426,10 @@ LaunchCache& cache() {
     return c;
 }
 
-template <int D, int PPT, int ACC, Pass PASS, int NT, int MINB, bool PREF>
+template <int D, int PPT, int ACC, Pass PASS, int NT, int MINB, bool PREF, bool PRUNE = false>
 int launch_lowd_v(const FusedF32& a, cudaStream_t s) {
     constexpr int VW = PPT < 4 ? PPT : 4;
-    auto kern = lowd_kernel<D, PPT, ACC, PASS, NT, MINB, PREF>;
+    auto kern = lowd_kernel<D, PPT, ACC, PASS, NT, MINB, PREF, PRUNE>;
     const size_t smem = lowd_smem_bytes(D, a.k, ACC, PASS, NT);
     const DeviceInfo& di = device_info();
     if (smem > di.smem_optin) return fail(CKM_ERR_UNSUPPORTED, "lowd: shared-memory table too large");
@@ -427,6 +513,12 @@ int launch_lowd_acc(const FusedF32& a, cudaStream_t s) {
         }
     }
     const int acc = choose_acc(D, a.k, PASS);
+    if constexpr (PASS != Pass::SumsOnly && D <= 8) {
+        if ((a.flags & FUSED_BOX_PRUNE) && a.k <= 32) {
+            if (acc == 0) return launch_lowd_v<D, PPT, 0, PASS, BLK, 2, false, true>(a, s);
+            if (acc == 1) return launch_lowd_v<D, PPT, 1, PASS, BLK, 2, true, true>(a, s);
+        }
+    }
     if (acc == 0) return launch_lowd_v<D, PPT, 0, PASS, BLK, 2, false>(a, s);
     if (acc == 1) return launch_lowd_v<D, PPT, 1, PASS, BLK, 2, true>(a, s);
     return fail(CKM_ERR_UNSUPPORTED, "lowd: no accumulation layout fits");

@@ -105,6 +105,26 @@ int ckm_fused_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clust
                   uint64_t *labels, uint64_t *masses, void *scratch, size_t scratch_bytes,
                   int mode, ckm_stream_t stream);
 
+/* Spatially ordered point sets (no counterpart in the reference; a layout
+ * of the same points).  ckm_spatial_sort_f32 writes a copy of the
+ * column-major points in Z-order of 2^16 cells of their bounding box
+ * (1 <= d <= 16, n < 2^32) and perm[q] = the caller's index of sorted point q.
+ * ckm_fused_sorted_f32 is ckm_fused_f32 (same contract, same labels, masses
+ * and centroids for the points it is given) that, for d <= 8 and k <= 32,
+ * skips per warp the clusters provably farther than another from all of the
+ * warp's points; on a spatially ordered set most clusters are skipped.  Its
+ * labels follow the order of the points it is given; ckm_unpermute_u32
+ * brings them to the caller's order (out[perm[q]] = in[q]). */
+size_t ckm_spatial_sort_workspace_bytes(void);
+int ckm_spatial_sort_f32(uint32_t num_features, uint64_t num_points, const float *points, float *sorted_points,
+                         uint32_t *perm, void *workspace, size_t workspace_bytes, ckm_stream_t stream);
+int ckm_fused_sorted_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                         const float *points, const float *old_centroids, float *new_centroids,
+                         uint32_t *labels, uint32_t *masses, void *scratch, size_t scratch_bytes,
+                         int mode, ckm_stream_t stream);
+int ckm_unpermute_u32(uint64_t num_points, const uint32_t *perm, const uint32_t *in, uint32_t *out,
+                      ckm_stream_t stream);
+
 /* The same fused iteration for callers that cannot allocate device memory
  * (a plugin inside a framework that owns all device memory, a loop that
  * must never call cudaMalloc/cudaFree, a caller given only its buffers).
