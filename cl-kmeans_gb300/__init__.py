@@ -63,6 +63,7 @@ class RunConfig(ctypes.Structure):
         ("chunk_bytes", ctypes.c_uint64),
         ("converge", ctypes.c_int),
         ("tolerance", ctypes.c_double),
+        ("spatial_order", ctypes.c_int),
     ]
 
 
@@ -132,7 +133,7 @@ def lib():
                                 ctypes.POINTER(RunInfo)], i32),
         "ckm_kmeans_run_f64": ([ctypes.POINTER(RunConfig), u32, u32, u64, u32, vp, vp, vp, vp,
                                 ctypes.POINTER(RunInfo)], i32),
-        "ckm_spatial_sort_workspace_bytes": ([], sz),
+        "ckm_spatial_sort_workspace_bytes": ([u64, u32], sz),
         "ckm_spatial_sort_f32": ([u32, u64, vp, vp, vp, vp, sz, vp], i32),
         "ckm_fused_sorted_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
         "ckm_unpermute_u32": ([u64, vp, vp, vp, vp], i32),
@@ -197,7 +198,7 @@ def spatial_sort(points, n, d, stream=None):
     L = lib()
     out = torch.empty_like(points)
     perm = torch.empty(n, dtype=torch.int32, device=points.device)
-    ws = torch.empty(int(L.ckm_spatial_sort_workspace_bytes()), dtype=torch.uint8, device=points.device)
+    ws = torch.empty(int(L.ckm_spatial_sort_workspace_bytes(n, d)), dtype=torch.uint8, device=points.device)
     check(L.ckm_spatial_sort_f32(d, n, _p(points), _p(out), _p(perm), _p(ws), ws.numel(), _stream(stream)),
           "ckm_spatial_sort_f32")
     return out, perm
@@ -272,7 +273,7 @@ def launch_count():
 def kmeans_run(points, d, k, iterations, centroids, pipeline="single_stage", fused_strategy="feature_sum",
                labeling_strategy="unroll_vector", mass_update_strategy="part_local",
                centroid_update_strategy="feature_sum", device=0, device_budget_bytes=0, chunk_bytes=0,
-               masses=None, labels=None, converge=False, tolerance=0.0):
+               masses=None, labels=None, converge=False, tolerance=0.0, spatial_order=0):
     """AbstractKmeans::operator() over HOST numpy arrays (column-major flat
     points and centroids).  converge: stop once the relative centroid shift
     falls below tolerance (default 1e-4).  Returns (centroids, masses,
@@ -287,7 +288,7 @@ def kmeans_run(points, d, k, iterations, centroids, pipeline="single_stage", fus
     Lb = np.zeros(n, it) if labels is None else labels
     cfg = RunConfig(pipeline.encode(), fused_strategy.encode(), labeling_strategy.encode(),
                     mass_update_strategy.encode(), centroid_update_strategy.encode(), device,
-                    device_budget_bytes, chunk_bytes, 1 if converge else 0, float(tolerance))
+                    device_budget_bytes, chunk_bytes, 1 if converge else 0, float(tolerance), int(spatial_order))
     info = RunInfo()
     fn = lib().ckm_kmeans_run_f64 if f64 else lib().ckm_kmeans_run_f32
     check(fn(ctypes.byref(cfg), iterations, d, n, k, P.ctypes.data, C.ctypes.data, M.ctypes.data,

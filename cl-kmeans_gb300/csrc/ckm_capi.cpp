@@ -185,7 +185,7 @@ int ckm_fused_sorted_f32(uint32_t d, uint64_t n, uint32_t k, const float* points
     return launch_generic_f32(a, Pass::Fused, s);
 }
 
-size_t ckm_spatial_sort_workspace_bytes(void) { return spatial_sort_workspace_bytes(); }
+size_t ckm_spatial_sort_workspace_bytes(uint64_t n, uint32_t d) { return spatial_sort_workspace_bytes(n, d); }
 
 int ckm_spatial_sort_f32(uint32_t d, uint64_t n, const float* points, float* sorted_points, uint32_t* perm,
                          void* workspace, size_t workspace_bytes, ckm_stream_t stream) {
@@ -195,8 +195,8 @@ int ckm_spatial_sort_f32(uint32_t d, uint64_t n, const float* points, float* sor
         return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: NULL pointer");
     if (points == sorted_points && n > 0)
         return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: sorted_points must not alias points");
-    if (!workspace || workspace_bytes < spatial_sort_workspace_bytes())
-        return fail(CKM_ERR_SCRATCH_TOO_SMALL, "spatial sort: workspace smaller than ckm_spatial_sort_workspace_bytes()");
+    if (!workspace || workspace_bytes < spatial_sort_workspace_bytes(n, d))
+        return fail(CKM_ERR_SCRATCH_TOO_SMALL, "spatial sort: workspace smaller than ckm_spatial_sort_workspace_bytes(n, d)");
     return launch_spatial_sort(d, n, points, sorted_points, perm, workspace, (cudaStream_t)stream);
 }
 

@@ -86,8 +86,8 @@ enum class Pass { Fused, LabelOnly, SumsOnly };
 
 // Launchers (return CKM_OK or an error status; never throw).
 int launch_fused_f32(const FusedF32& a, Pass pass, cudaStream_t s);
-// Spatial order (ckm_spatial.cu): counting sort by a Z-order cell key.
-size_t spatial_sort_workspace_bytes();
+// Spatial order (ckm_spatial.cu): radix sort by a Z-order cell key.
+size_t spatial_sort_workspace_bytes(uint64_t n, uint32_t d);
 int launch_spatial_sort(uint32_t d, uint64_t n, const float* points, float* sorted, uint32_t* perm, void* ws,
                         cudaStream_t s);
 int launch_unpermute_u32(uint64_t n, const uint32_t* perm, const uint32_t* in, uint32_t* out, cudaStream_t s);

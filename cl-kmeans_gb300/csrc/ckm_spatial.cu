@@ -1,7 +1,7 @@
 // Spatial order for the low-d fused kernel's box pruning.
 //
-// A counting sort of the points by a 16-bit Z-order (Morton) key of their
-// cells: each feature's range [min, max] is cut into 2^b bins
+// A stable LSD radix sort of the points by a 16-bit Z-order (Morton) key of
+// their cells: each feature's range [min, max] is cut into 2^b bins
 // (b = max(1, 16 / d) for d <= 16), and the bins' bits interleave into the
 // key, so consecutive keys are neighbouring cells.  After the sort every
 // 256-point warp tile of the fused kernel covers one or a few small cells, and
@@ -10,11 +10,16 @@
 // of the arithmetic: labels computed on the sorted set go back to the caller's
 // order through the permutation (unpermute).
 //
-//   bbox:    per-feature min / max (order-preserving integer atomics)
-//   count:   points per key (warp-aggregated global atomics)
-//   scan:    exclusive prefix of the 65536 counts (one CTA)
-//   scatter: position = start of the key + running count (warp-aggregated),
-//            sorted[f * n + pos] = points[f * n + p], perm[pos] = p
+//   bbox:      per-feature min / max (order-preserving integer atomics)
+//   per pass (8 key bits, low byte first; the key is recomputed from the
+//   point, and the points and their original indices travel with it):
+//   upsweep:   per chunk (CHUNK consecutive items), the count of each digit
+//   scan:      exclusive prefix of the counts in digit-major order: where each
+//              (digit, chunk) run starts in the output
+//   downsweep: each CTA ranks its chunk's items by digit, stably, in shared
+//              memory (rounds of 256 items, warp match + per-warp counts), and
+//              writes each digit's run contiguously (coalesced), gathering
+//              the points from the chunk it has just read
 #include <cuda_runtime.h>
 
 #include "ckm_device.cuh"
@@ -23,7 +28,6 @@
 namespace ckm {
 namespace {
 
-constexpr uint32_t KEY_BINS = 1u << 16;
 constexpr int SB = 256;
 
 __device__ __forceinline__ uint32_t ord_of(float x) {
@@ -34,18 +38,45 @@ __device__ __forceinline__ float float_of(uint32_t u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-// ws layout: [0, 16) min (ordered), [16, 32) max (ordered), then counts
-// [KEY_BINS], then cursors [KEY_BINS].
+// Workspace: [0, 16) min (ordered), [16, 32) max (ordered), the counts /
+// offsets [RADIX * chunks], the scan's block sums, then the intermediate
+// points [d * n] and indices [n] between the two passes.
+constexpr uint32_t RADIX = 256;
+constexpr uint32_t SCAN_PER_BLOCK = 4096;
+
 struct SortWs {
     uint32_t* lo;
     uint32_t* hi;
     uint32_t* counts;
-    uint32_t* cursor;
+    uint32_t* block_sums;
+    float* tmp_points;
+    uint32_t* tmp_idx;
 };
 
-SortWs sort_ws(void* ws) {
-    uint32_t* w = static_cast<uint32_t*>(ws);
-    return SortWs{w, w + 16, w + 32, w + 32 + KEY_BINS};
+// Items per chunk: the chunk is re-read (gathered) from L2 when written out, so
+// it stays a 64 KiB window of points.
+uint32_t chunk_items(uint32_t d) { return d <= 4 ? 4096u : (d <= 8 ? 2048u : 1024u); }
+
+uint64_t num_chunks(uint64_t n, uint32_t d) { return (n + chunk_items(d) - 1) / chunk_items(d); }
+
+size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
+
+uint64_t scan_blocks_of(uint64_t n, uint32_t d) {
+    return ((uint64_t)RADIX * num_chunks(n, d) + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+}
+
+SortWs sort_ws(void* ws, uint64_t n, uint32_t d) {
+    unsigned char* w = static_cast<unsigned char*>(ws);
+    const size_t counts = a256((size_t)RADIX * num_chunks(n, d) * 4);
+    const size_t sums = a256((size_t)scan_blocks_of(n, d) * 4);
+    SortWs r;
+    r.lo = reinterpret_cast<uint32_t*>(w);
+    r.hi = r.lo + 16;
+    r.counts = reinterpret_cast<uint32_t*>(w + 256);
+    r.block_sums = reinterpret_cast<uint32_t*>(w + 256 + counts);
+    r.tmp_points = reinterpret_cast<float*>(w + 256 + counts + sums);
+    r.tmp_idx = reinterpret_cast<uint32_t*>(w + 256 + counts + sums + a256((size_t)n * d * 4));
+    return r;
 }
 
 __global__ void __launch_bounds__(SB) bbox_kernel(const float* __restrict__ P, uint64_t n, uint32_t d, SortWs ws) {
@@ -100,62 +131,206 @@ __device__ __forceinline__ void load_range(const SortWs& ws, uint32_t d, uint32_
     }
 }
 
-__global__ void __launch_bounds__(SB) count_kernel(const float* __restrict__ P, uint64_t n, uint32_t d, uint32_t b,
-                                                   SortWs ws) {
+// Digit (8 bits at `shift`) of item i of a pass's input.
+__device__ __forceinline__ uint32_t item_digit(const float* __restrict__ P, uint64_t n, uint64_t i, uint32_t d,
+                                               uint32_t b, const float* lo, const float* scale, uint32_t shift) {
+    return (point_key(P, n, i, d, b, lo, scale) >> shift) & (RADIX - 1u);
+}
+
+// Digit histogram of one chunk into s_hist (warp-aggregated shared atomics);
+// every thread of the CTA calls it.
+__device__ __forceinline__ void chunk_histogram(const float* __restrict__ P, uint64_t n, uint32_t d, uint32_t b,
+                                                const float* lo, const float* scale, uint32_t shift, uint64_t c0,
+                                                uint32_t chunk, uint32_t* s_hist) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t j = threadIdx.x; j < RADIX; j += SB) s_hist[j] = 0u;
+    __syncthreads();
+    for (uint32_t r = 0; r < chunk; r += SB) {
+        const uint64_t i = c0 + r + threadIdx.x;
+        const bool ok = i < n;
+        const uint32_t active = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint32_t dg = item_digit(P, n, i, d, b, lo, scale, shift);
+            const uint32_t peers = __match_any_sync(active, dg);
+            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_hist[dg], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SB) upsweep_kernel(const float* __restrict__ P, uint64_t n, uint32_t d, uint32_t b,
+                                                     SortWs ws, uint32_t shift, uint32_t chunk, uint64_t chunks) {
+    __shared__ uint32_t s_hist[RADIX];
     float lo[16], scale[16];
     load_range(ws, d, b, lo, scale);
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint64_t base = (uint64_t)blockIdx.x * SB + (threadIdx.x & ~31u); base < n; base += (uint64_t)gridDim.x * SB) {
-        const uint64_t p = base + lane;
-        const bool ok = p < n;
-        const uint32_t active = __ballot_sync(0xffffffffu, ok);
-        if (!ok) continue;
-        const uint32_t key = point_key(P, n, p, d, b, lo, scale);
-        const uint32_t peers = __match_any_sync(active, key);
-        if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&ws.counts[key], (uint32_t)__popc(peers));
+    const uint64_t c = blockIdx.x;
+    chunk_histogram(P, n, d, b, lo, scale, shift, c * chunk, chunk, s_hist);
+    for (uint32_t j = threadIdx.x; j < RADIX; j += SB) ws.counts[(uint64_t)j * chunks + c] = s_hist[j];
+}
+
+// Exclusive scan of counts[0, m) in place: block sums, then their scan, then
+// each block's prefix.
+__global__ void __launch_bounds__(SB) scan_sums_kernel(const uint32_t* __restrict__ v, uint64_t m, uint32_t* sums) {
+    __shared__ uint32_t s_w[SB / 32];
+    const uint64_t b0 = (uint64_t)blockIdx.x * SCAN_PER_BLOCK;
+    uint32_t t = 0;
+    for (uint32_t j = threadIdx.x; j < SCAN_PER_BLOCK; j += SB)
+        if (b0 + j < m) t += v[b0 + j];
+    t = __reduce_add_sync(0xffffffffu, t);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int w = 0; w < SB / 32; ++w) s += s_w[w];
+        sums[blockIdx.x] = s;
     }
 }
 
-__global__ void __launch_bounds__(1024) scan_kernel(SortWs ws) {
-    // 65536 counts, 64 per thread: exclusive prefix into cursor
+__global__ void __launch_bounds__(1024) scan_block_sums_kernel(uint32_t* sums, uint32_t nb) {
+    // exclusive scan of nb values: each thread a run of ceil(nb / 1024)
     __shared__ uint32_t s_part[1024];
     const uint32_t t = threadIdx.x;
-    uint32_t sum = 0;
-    for (uint32_t i = 0; i < 64; ++i) sum += ws.counts[t * 64 + i];
-    s_part[t] = sum;
+    const uint32_t per = (nb + 1023u) / 1024u;
+    const uint32_t j0 = t * per;
+    uint32_t tot = 0;
+    for (uint32_t i = 0; i < per; ++i)
+        if (j0 + i < nb) tot += sums[j0 + i];
+    s_part[t] = tot;
     __syncthreads();
     for (uint32_t o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = t >= o ? s_part[t - o] : 0u;
+        const uint32_t x = t >= o ? s_part[t - o] : 0u;
         __syncthreads();
-        s_part[t] += v;
+        s_part[t] += x;
         __syncthreads();
     }
-    uint32_t run = s_part[t] - sum;  // exclusive
-    for (uint32_t i = 0; i < 64; ++i) {
-        ws.cursor[t * 64 + i] = run;
-        run += ws.counts[t * 64 + i];
+    uint32_t run = s_part[t] - tot;
+    for (uint32_t i = 0; i < per; ++i)
+        if (j0 + i < nb) {
+            const uint32_t v = sums[j0 + i];
+            sums[j0 + i] = run;
+            run += v;
+        }
+}
+
+__global__ void __launch_bounds__(SB) scan_apply_kernel(uint32_t* v, uint64_t m, const uint32_t* __restrict__ sums) {
+    // per block: 16 consecutive values per thread, a block scan of the
+    // thread totals, plus the block's offset
+    __shared__ uint32_t s_part[SB];
+    const uint64_t b0 = (uint64_t)blockIdx.x * SCAN_PER_BLOCK;
+    const uint32_t per = SCAN_PER_BLOCK / SB;
+    const uint64_t j0 = b0 + (uint64_t)threadIdx.x * per;
+    uint32_t x[SCAN_PER_BLOCK / SB], tot = 0;
+    for (uint32_t i = 0; i < per; ++i) {
+        x[i] = j0 + i < m ? v[j0 + i] : 0u;
+        tot += x[i];
+    }
+    s_part[threadIdx.x] = tot;
+    __syncthreads();
+    for (uint32_t o = 1; o < SB; o <<= 1) {
+        const uint32_t y = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s_part[threadIdx.x] += y;
+        __syncthreads();
+    }
+    uint32_t run = sums[blockIdx.x] + s_part[threadIdx.x] - tot;
+    for (uint32_t i = 0; i < per; ++i) {
+        if (j0 + i < m) v[j0 + i] = run;
+        run += x[i];
     }
 }
 
-__global__ void __launch_bounds__(SB) scatter_kernel(const float* __restrict__ P, uint64_t n, uint32_t d, uint32_t b,
-                                                     SortWs ws, float* __restrict__ out, uint32_t* __restrict__ perm) {
+// One pass's scatter for one chunk:
+//   1. the chunk's items are read once (coalesced); their digits go to shared
+//      memory and into the chunk's histogram;
+//   2. the items are ranked stably within their digits in rounds of SB (item
+//      order = round, then thread; warp match + per-warp counts), entirely in
+//      shared memory: s_src[pos] = the chunk-local index of the item at
+//      position pos of the chunk sorted by digit;
+//   3. the sorted chunk is written out digit run by digit run (consecutive
+//      output positions, coalesced), gathering the point values from the
+//      chunk just read (an L2-resident window).
+__global__ void __launch_bounds__(SB) downsweep_kernel(const float* __restrict__ P, const uint32_t* __restrict__ idx_in,
+                                                       uint64_t n, uint32_t d, uint32_t b, SortWs ws, uint32_t shift,
+                                                       uint32_t chunk, uint64_t chunks, float* __restrict__ P_out,
+                                                       uint32_t* __restrict__ idx_out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint16_t* s_src = reinterpret_cast<uint16_t*>(smem);                 // [chunk]
+    unsigned char* s_din = reinterpret_cast<unsigned char*>(s_src + chunk);  // digit of local item j
+    unsigned char* s_dig = s_din + chunk;                                 // digit at sorted position
+    __shared__ uint32_t s_hist[RADIX], s_off[RADIX], s_run[RADIX], s_wcnt[SB / 32][RADIX];
     float lo[16], scale[16];
     load_range(ws, d, b, lo, scale);
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint64_t base = (uint64_t)blockIdx.x * SB + (threadIdx.x & ~31u); base < n; base += (uint64_t)gridDim.x * SB) {
-        const uint64_t p = base + lane;
-        const bool ok = p < n;
+    const uint64_t c = blockIdx.x;
+    const uint64_t c0 = c * chunk;
+    const uint32_t valid = (uint32_t)min((uint64_t)chunk, n - c0);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+
+    // 1. digits and histogram
+    s_hist[threadIdx.x] = 0u;
+    s_run[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t r = 0; r < chunk; r += SB) {
+        const uint32_t j = r + threadIdx.x;
+        const bool ok = j < valid;
         const uint32_t active = __ballot_sync(0xffffffffu, ok);
-        if (!ok) continue;
-        const uint32_t key = point_key(P, n, p, d, b, lo, scale);
-        const uint32_t peers = __match_any_sync(active, key);
-        const uint32_t leader = __ffs(peers) - 1;
-        uint32_t start = 0;
-        if (lane == leader) start = atomicAdd(&ws.cursor[key], (uint32_t)__popc(peers));
-        start = __shfl_sync(peers, start, leader);
-        const uint32_t pos = start + __popc(peers & ((1u << lane) - 1u));
-        for (uint32_t f = 0; f < d; ++f) out[(size_t)f * n + pos] = __ldg(P + (size_t)f * n + p);
-        perm[pos] = (uint32_t)p;
+        if (ok) {
+            const uint32_t dg = item_digit(P, n, c0 + j, d, b, lo, scale, shift);
+            s_din[j] = (unsigned char)dg;
+            const uint32_t peers = __match_any_sync(active, dg);
+            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_hist[dg], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    // exclusive scan of the histogram (SB == RADIX: one digit per thread)
+    s_off[threadIdx.x] = s_hist[threadIdx.x];
+    __syncthreads();
+    for (uint32_t o = 1; o < RADIX; o <<= 1) {
+        const uint32_t y = threadIdx.x >= o ? s_off[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s_off[threadIdx.x] += y;
+        __syncthreads();
+    }
+    s_off[threadIdx.x] -= s_hist[threadIdx.x];
+    __syncthreads();
+
+    // 2. stable ranks
+    for (uint32_t r = 0; r < valid; r += SB) {
+        const uint32_t j = r + threadIdx.x;
+        const bool ok = j < valid;
+        const uint32_t active = __ballot_sync(0xffffffffu, ok);
+        for (uint32_t t = lane; t < RADIX; t += 32) s_wcnt[warp][t] = 0u;
+        __syncwarp();  // the row is zero before any leader writes its count
+        uint32_t dg = 0, rank = 0;
+        if (ok) {
+            dg = s_din[j];
+            const uint32_t peers = __match_any_sync(active, dg);
+            rank = __popc(peers & ((1u << lane) - 1u));
+            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wcnt[warp][dg] = __popc(peers);
+        }
+        __syncthreads();
+        if (ok) {
+            uint32_t pre = s_run[dg];
+            for (uint32_t w = 0; w < warp; ++w) pre += s_wcnt[w][dg];
+            const uint32_t pos = s_off[dg] + pre + rank;
+            s_src[pos] = (uint16_t)j;
+            s_dig[pos] = (unsigned char)dg;
+        }
+        __syncthreads();
+        {
+            uint32_t add = 0;
+            for (uint32_t w = 0; w < SB / 32; ++w) add += s_wcnt[w][threadIdx.x];
+            s_run[threadIdx.x] += add;
+        }
+        __syncthreads();
+    }
+
+    // 3. write out
+    for (uint32_t q = threadIdx.x; q < valid; q += SB) {
+        const uint32_t dg = s_dig[q];
+        const uint32_t src = s_src[q];
+        const uint64_t g = (uint64_t)ws.counts[(uint64_t)dg * chunks + c] + (q - s_off[dg]);
+        for (uint32_t f = 0; f < d; ++f) P_out[(size_t)f * n + g] = __ldg(P + (size_t)f * n + c0 + src);
+        idx_out[g] = idx_in ? __ldg(idx_in + c0 + src) : (uint32_t)(c0 + src);
     }
 }
 
@@ -174,23 +349,57 @@ uint32_t grid_of(uint64_t n) {
 
 }  // namespace
 
-size_t spatial_sort_workspace_bytes() { return (32 + 2 * (size_t)KEY_BINS) * sizeof(uint32_t); }
+size_t spatial_sort_workspace_bytes(uint64_t n, uint32_t d) {
+    if (d == 0) return 0;
+    return 256 + a256((size_t)RADIX * num_chunks(n, d) * 4) + a256((size_t)scan_blocks_of(n, d) * 4) +
+           a256((size_t)n * d * 4) + a256((size_t)n * 4);
+}
+
+namespace {
+size_t downsweep_smem(uint32_t d) { return (size_t)chunk_items(d) * 4; }  // s_src (u16) + two digit arrays
+}  // namespace
 
 int launch_spatial_sort(uint32_t d, uint64_t n, const float* points, float* sorted, uint32_t* perm, void* ws_ptr,
                         cudaStream_t s) {
-    SortWs ws = sort_ws(ws_ptr);
-    // lo = all ones (min identity), hi and the counts = zero
+    SortWs ws = sort_ws(ws_ptr, n, d);
+    // lo = all ones (min identity), hi = zero
     cudaError_t e = cudaMemsetAsync(ws.lo, 0xff, 16 * sizeof(uint32_t), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ws.hi, 0, (16 + 2 * (size_t)KEY_BINS) * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ws.hi, 0, 16 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return cuda_fail(e, "spatial sort: workspace init");
     if (n == 0) return CKM_OK;
     const uint32_t b = d >= 16 ? 1u : 16u / d;
-    const uint32_t g = grid_of(n);
-    bbox_kernel<<<g, SB, 0, s>>>(points, n, d, ws);
-    count_kernel<<<g, SB, 0, s>>>(points, n, d, b, ws);
-    scan_kernel<<<1, 1024, 0, s>>>(ws);
-    scatter_kernel<<<g, SB, 0, s>>>(points, n, d, b, ws, sorted, perm);
-    count_launch(4);
+    const uint32_t chunk = chunk_items(d);
+    const uint64_t chunks = num_chunks(n, d);
+    const uint64_t m = (uint64_t)RADIX * chunks;
+    const uint64_t scan_blocks = scan_blocks_of(n, d);
+    const size_t smem = downsweep_smem(d);
+    static bool attr_done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, downsweep_kernel);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(spatial downsweep)");
+        e = cudaFuncSetAttribute(downsweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(device_info().smem_optin - fa.sharedSizeBytes));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(spatial downsweep)");
+        attr_done[dev] = true;
+    }
+    bbox_kernel<<<grid_of(n), SB, 0, s>>>(points, n, d, ws);
+    for (uint32_t pass = 0; pass < 2; ++pass) {
+        const uint32_t shift = 8 * pass;
+        const float* src = pass == 0 ? points : ws.tmp_points;
+        const uint32_t* src_idx = pass == 0 ? nullptr : ws.tmp_idx;
+        float* dst = pass == 0 ? ws.tmp_points : sorted;
+        uint32_t* dst_idx = pass == 0 ? ws.tmp_idx : perm;
+        upsweep_kernel<<<(unsigned)chunks, SB, 0, s>>>(src, n, d, b, ws, shift, chunk, chunks);
+        scan_sums_kernel<<<(unsigned)scan_blocks, SB, 0, s>>>(ws.counts, m, ws.block_sums);
+        scan_block_sums_kernel<<<1, 1024, 0, s>>>(ws.block_sums, (uint32_t)scan_blocks);
+        scan_apply_kernel<<<(unsigned)scan_blocks, SB, 0, s>>>(ws.counts, m, ws.block_sums);
+        downsweep_kernel<<<(unsigned)chunks, SB, smem, s>>>(src, src_idx, n, d, b, ws, shift, chunk, chunks, dst,
+                                                            dst_idx);
+    }
+    count_launch(11);
     e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "spatial sort launch");
 }

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "abstract_kmeans.hpp"
 #include "factories.hpp"
@@ -53,22 +54,64 @@ public:
         Timer::Timer total_timer;
         total_timer.start();
         this->reset_progress();
+        // spatial order: the iterations run on a Z-ordered copy of the points
+        // with per-warp box pruning (same labels per point, mapped back to
+        // the caller's order after the loop); the sort is inside the window
+        const bool spatial = use_spatial_order(d, n, k);
+        const PointT* iter_points = points_.data();
+        if (spatial) {
+            auto& dp = this->measurement->add_datapoint().set_name("SpatialSort");
+            Event& ev = dp.add_event(queue_);
+            sorted_points_.resize(n * d);
+            perm_.resize(n);
+            sort_ws_.resize(ckm_spatial_sort_workspace_bytes(n, (uint32_t)d));
+            ckm_check(ckm_spatial_sort_f32((uint32_t)d, n, reinterpret_cast<const float*>(points_.data()),
+                                           reinterpret_cast<float*>(sorted_points_.data()), perm_.data(),
+                                           sort_ws_.data(), sort_ws_.size(), queue_.get()),
+                      "SpatialSort");
+            ev.record_end(queue_);
+            iter_points = sorted_points_.data();
+        }
         for (uint32_t iteration = 0; iteration < this->max_iterations; ++iteration) {
-            engine_.launch(queue_, d, n, k, points_.data(), centroids_.data(), new_centroids_.data(),
-                           labels_.data(), masses_.data(), CKM_MODE_FINALIZE,
-                           this->measurement->add_datapoint((int)iteration), WaitList());
+            if (spatial) {
+                auto& dp = this->measurement->add_datapoint((int)iteration).set_name("FusedFeatureSumSorted");
+                Event& ev = dp.add_event(queue_);
+                Scratch& sc = engine_.scratch();
+                sc.reserve((uint32_t)d, (uint32_t)k, queue_);
+                ckm_check(ckm_fused_sorted_f32((uint32_t)d, n, (uint32_t)k,
+                                               reinterpret_cast<const float*>(iter_points),
+                                               reinterpret_cast<const float*>(centroids_.data()),
+                                               reinterpret_cast<float*>(new_centroids_.data()),
+                                               reinterpret_cast<uint32_t*>(labels_.data()),
+                                               reinterpret_cast<uint32_t*>(masses_.data()), sc.data(), sc.bytes(),
+                                               CKM_MODE_FINALIZE, queue_.get()),
+                          "FusedFeatureSumSorted");
+                ev.record_end(queue_);
+            } else {
+                engine_.launch(queue_, d, n, k, points_.data(), centroids_.data(), new_centroids_.data(),
+                               labels_.data(), masses_.data(), CKM_MODE_FINALIZE,
+                               this->measurement->add_datapoint((int)iteration), WaitList());
+            }
             centroids_.swap(new_centroids_);
             if (this->after_iteration(iteration, probe_, (uint32_t)d, (uint32_t)k, new_centroids_.data(),
                                       centroids_.data(), queue_))
                 break;
         }
+        if (spatial) {
+            // labels back to the caller's order
+            labels_out_.resize(n);
+            ckm_check(ckm_unpermute_u32(n, perm_.data(), reinterpret_cast<const uint32_t*>(labels_.data()),
+                                        reinterpret_cast<uint32_t*>(labels_out_.data()), queue_.get()),
+                      "UnpermuteLabels");
+        }
         queue_.finish();
         uint64_t total_time = total_timer.stop<std::chrono::nanoseconds>();
         this->measurement->add_datapoint().set_name("TotalTime").add_value() = total_time;
         last_total_ns_ = total_time;
+        last_spatial_ = spatial;
 
         download("CentroidsD2H", centroids_, this->io_centroids(), k * d);
-        download("LabelsD2H", labels_, this->out_labels(), n);
+        download("LabelsD2H", spatial ? labels_out_ : labels_, this->out_labels(), n);
         download("MassesD2H", masses_, this->out_masses(), k);
         queue_.finish();
         h2d_bytes_ = (n * d + k * d) * sizeof(PointT);
@@ -90,6 +133,12 @@ public:
         }
     }
 
+    // Spatial order of the iterations: 0 = auto (FP32, d <= 8, k <= 32,
+    // n >= 2^20, >= 8 iterations, enough free device memory), 1 = whenever
+    // the shape allows, -1 = never.
+    void set_spatial_order(int mode) { spatial_mode_ = mode; }
+    bool used_spatial_order() const { return last_spatial_; }
+
     uint64_t last_total_ns() const { return last_total_ns_; }
     uint64_t h2d_bytes() const { return h2d_bytes_; }
     uint64_t d2h_bytes() const { return d2h_bytes_; }
@@ -105,12 +154,31 @@ private:
         ev.record_end(queue_);
     }
 
+    bool use_spatial_order(size_t d, size_t n, size_t k) const {
+        if (spatial_mode_ < 0) return false;
+        if (!(std::is_same<PointT, float>::value && std::is_same<LabelT, uint32_t>::value &&
+              std::is_same<MassT, uint32_t>::value && ColMajor))
+            return false;
+        if (d < 1 || d > 8 || k > 32 || n == 0 || n > 0xffffffffull) return false;
+        if (spatial_mode_ > 0) return true;
+        if (n < (1ull << 20) || this->max_iterations < 8) return false;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+        const size_t need = n * d * sizeof(PointT) + n * 2 * sizeof(LabelT) +
+                            ckm_spatial_sort_workspace_bytes(n, (uint32_t)d);
+        return need + (size_t(1) << 30) < free_b;
+    }
+
     FusedLloyd<PointT, LabelT, MassT> engine_;
     ConvergenceProbe<PointT, LabelT, MassT> probe_;
     Stream queue_;
-    DeviceVector<PointT> points_, centroids_, new_centroids_;
-    DeviceVector<LabelT> labels_;
+    DeviceVector<PointT> points_, centroids_, new_centroids_, sorted_points_;
+    DeviceVector<LabelT> labels_, labels_out_;
     DeviceVector<MassT> masses_;
+    DeviceVector<uint32_t> perm_;
+    DeviceVector<unsigned char> sort_ws_;
+    int spatial_mode_ = 0;
+    bool last_spatial_ = false;
     uint64_t last_total_ns_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
 };
 

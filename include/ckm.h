@@ -108,14 +108,17 @@ int ckm_fused_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clust
 /* Spatially ordered point sets (no counterpart in the reference; a layout
  * of the same points).  ckm_spatial_sort_f32 writes a copy of the
  * column-major points in Z-order of 2^16 cells of their bounding box
- * (1 <= d <= 16, n < 2^32) and perm[q] = the caller's index of sorted point q.
+ * (1 <= d <= 16, n < 2^32; a stable radix sort, so equal cells keep the
+ * caller's order) and perm[q] = the caller's index of sorted point q.  Its
+ * workspace holds one more copy of the points and indices:
+ * ckm_spatial_sort_workspace_bytes(n, d) bytes.
  * ckm_fused_sorted_f32 is ckm_fused_f32 (same contract, same labels, masses
  * and centroids for the points it is given) that, for d <= 8 and k <= 32,
  * skips per warp the clusters provably farther than another from all of the
  * warp's points; on a spatially ordered set most clusters are skipped.  Its
  * labels follow the order of the points it is given; ckm_unpermute_u32
  * brings them to the caller's order (out[perm[q]] = in[q]). */
-size_t ckm_spatial_sort_workspace_bytes(void);
+size_t ckm_spatial_sort_workspace_bytes(uint64_t num_points, uint32_t num_features);
 int ckm_spatial_sort_f32(uint32_t num_features, uint64_t num_points, const float *points, float *sorted_points,
                          uint32_t *perm, void *workspace, size_t workspace_bytes, ckm_stream_t stream);
 int ckm_fused_sorted_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
@@ -358,6 +361,11 @@ typedef struct ckm_run_config {
     int converge;                          /* kmeans.converge: stop once the relative centroid shift
                                               (ckm_centroid_shift_*) falls below tolerance */
     double tolerance;                      /* 0 = 1e-4 */
+    int spatial_order;                     /* single_stage, FP32, d <= 8, k <= 32: run the iterations on
+                                              a spatially ordered copy (ckm_spatial_sort_f32, box-pruned
+                                              ckm_fused_sorted_f32; labels mapped back at the end).
+                                              0 = auto (n >= 2^20, >= 8 iterations, device memory
+                                              allows), 1 = whenever the shape allows, -1 = never */
 } ckm_run_config;
 
 typedef struct ckm_run_info {

@@ -118,6 +118,20 @@ def test_pipelines_end_to_end(ckm, oracle, cuda, pipeline):
     _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L)
 
 
+@pytest.mark.parametrize("n,d,k,iters,mode", [(100003, 4, 10, 12, 1), (1 << 20, 4, 16, 10, 0), (60000, 2, 7, 9, 1),
+                                              (50001, 8, 32, 8, 1), (40000, 3, 40, 6, 1)])
+def test_single_stage_spatial_order(ckm, oracle, cuda, n, d, k, iters, mode):
+    """single_stage with spatial_order = 1 (whenever the shape allows) or
+    0 (auto: n >= 2^20): the iterations run on a sorted copy with box pruning
+    and the labels come back in the caller's order; results as the oracle's.
+    k = 40 is outside the pruned shapes and runs the caller's order."""
+    P = blobs(n, d, k, seed=n + k)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    C, M, L, info = ckm.kmeans_run(P, d, k, iters, C0, pipeline="single_stage", spatial_order=mode)
+    assert info.iterations == iters
+    _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L.view(np.uint32))
+
+
 def test_pipeline_double_types(ckm, oracle, cuda):
     n, d, k, iters = 20000, 3, 6, 5
     P = blobs(n, d, k, seed=98).astype(np.float64)
