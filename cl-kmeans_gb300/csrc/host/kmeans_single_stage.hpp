@@ -72,8 +72,12 @@ public:
             ev.record_end(queue_);
             iter_points = sorted_points_.data();
         }
+        bool labels_sorted = false;  // labels_ holds the sorted set's order
         for (uint32_t iteration = 0; iteration < this->max_iterations; ++iteration) {
-            if (spatial) {
+            // the last iteration of a full run labels the caller's order
+            // directly (the same labels per point), so no unpermute is needed
+            if (spatial && iteration + 1 < this->max_iterations) {
+                labels_sorted = true;
                 auto& dp = this->measurement->add_datapoint((int)iteration).set_name("FusedFeatureSumSorted");
                 Event& ev = dp.add_event(queue_);
                 Scratch& sc = engine_.scratch();
@@ -88,6 +92,7 @@ public:
                           "FusedFeatureSumSorted");
                 ev.record_end(queue_);
             } else {
+                labels_sorted = false;
                 engine_.launch(queue_, d, n, k, points_.data(), centroids_.data(), new_centroids_.data(),
                                labels_.data(), masses_.data(), CKM_MODE_FINALIZE,
                                this->measurement->add_datapoint((int)iteration), WaitList());
@@ -97,8 +102,9 @@ public:
                                       centroids_.data(), queue_))
                 break;
         }
-        if (spatial) {
-            // labels back to the caller's order
+        if (labels_sorted) {
+            // stopped early on the convergence test: labels back to the
+            // caller's order
             labels_out_.resize(n);
             ckm_check(ckm_unpermute_u32(n, perm_.data(), reinterpret_cast<const uint32_t*>(labels_.data()),
                                         reinterpret_cast<uint32_t*>(labels_out_.data()), queue_.get()),
@@ -111,7 +117,7 @@ public:
         last_spatial_ = spatial;
 
         download("CentroidsD2H", centroids_, this->io_centroids(), k * d);
-        download("LabelsD2H", spatial ? labels_out_ : labels_, this->out_labels(), n);
+        download("LabelsD2H", labels_sorted ? labels_out_ : labels_, this->out_labels(), n);
         download("MassesD2H", masses_, this->out_masses(), k);
         queue_.finish();
         h2d_bytes_ = (n * d + k * d) * sizeof(PointT);

@@ -132,6 +132,19 @@ def test_single_stage_spatial_order(ckm, oracle, cuda, n, d, k, iters, mode):
     _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L.view(np.uint32))
 
 
+def test_single_stage_spatial_order_converging(ckm, oracle, cuda):
+    """A spatial-order run that stops on the convergence test before the
+    iteration cap ends on the sorted set; its labels are mapped back to the
+    caller's order and equal the oracle's for that many iterations."""
+    n, d, k = 100003, 4, 10
+    P = blobs(n, d, k, seed=5)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    C, M, L, info = ckm.kmeans_run(P, d, k, 60, C0, pipeline="single_stage", spatial_order=1, converge=True,
+                                   tolerance=1e-4)
+    assert info.converged == 1 and info.iterations < 60
+    _e2e_check(oracle, P, n, d, k, int(info.iterations), C0, C, M, L.view(np.uint32))
+
+
 def test_pipeline_double_types(ckm, oracle, cuda):
     n, d, k, iters = 20000, 3, 6, 5
     P = blobs(n, d, k, seed=98).astype(np.float64)
