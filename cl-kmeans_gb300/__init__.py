@@ -38,6 +38,7 @@ EXPORTS = [
     "ckm_finalize_f32", "ckm_finalize_f64", "ckm_generate_mixture_f32",
     "ckm_kmeans_run_f32", "ckm_kmeans_run_f64",
     "ckm_spatial_sort_workspace_bytes", "ckm_spatial_sort_f32", "ckm_fused_sorted_f32", "ckm_unpermute_u32",
+    "ckm_labeling_sorted_f32",
 ]
 
 
@@ -137,6 +138,7 @@ def lib():
         "ckm_spatial_sort_f32": ([u32, u64, vp, vp, vp, vp, sz, vp], i32),
         "ckm_fused_sorted_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),
         "ckm_unpermute_u32": ([u64, vp, vp, vp, vp], i32),
+        "ckm_labeling_sorted_f32": ([u32, u64, u32, vp, vp, vp, vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)

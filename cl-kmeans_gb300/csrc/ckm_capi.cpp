@@ -185,6 +185,20 @@ int ckm_fused_sorted_f32(uint32_t d, uint64_t n, uint32_t k, const float* points
     return launch_generic_f32(a, Pass::Fused, s);
 }
 
+int ckm_labeling_sorted_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, const float* centroids,
+                            uint32_t* labels, ckm_stream_t stream) {
+    int st = check_shape(d, n, k);
+    if (st) return st;
+    if (n == 0) return CKM_OK;
+    if (!points || !centroids || !labels) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL pointer");
+    FusedF32 a{points, centroids, labels, nullptr, nullptr, ScratchView{nullptr, nullptr, nullptr}, n, d, k,
+               CKM_MODE_DEFER};
+    a.flags = FUSED_BOX_PRUNE;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (lowd_supported(d, k)) return launch_fused_f32(a, Pass::LabelOnly, s);
+    return launch_generic_f32(a, Pass::LabelOnly, s);
+}
+
 size_t ckm_spatial_sort_workspace_bytes(uint64_t n, uint32_t d) { return spatial_sort_workspace_bytes(n, d); }
 
 int ckm_spatial_sort_f32(uint32_t d, uint64_t n, const float* points, float* sorted_points, uint32_t* perm,

@@ -106,6 +106,25 @@ private:
     DeviceVector<unsigned char> buf_;
 };
 
+// Whether a run uses the spatially ordered copy of its points (FP32,
+// column-major, d <= 8, k <= 32, n < 2^32).  mode: 0 = auto (additionally
+// n >= 2^20, >= 8 iterations and enough free device memory), 1 = whenever the
+// shape allows, -1 = never.
+template <typename PointT, typename LabelT, typename MassT, bool ColMajor>
+bool spatial_order_eligible(int mode, size_t d, size_t n, size_t k, uint32_t iterations) {
+    if (mode < 0) return false;
+    if (!(std::is_same<PointT, float>::value && std::is_same<LabelT, uint32_t>::value &&
+          std::is_same<MassT, uint32_t>::value && ColMajor))
+        return false;
+    if (d < 1 || d > 8 || k > 32 || n == 0 || n > 0xffffffffull) return false;
+    if (mode > 0) return true;
+    if (n < (1ull << 20) || iterations < 8) return false;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+    const size_t need = n * d * sizeof(PointT) + n * 2 * sizeof(LabelT) + ckm_spatial_sort_workspace_bytes(n, (uint32_t)d);
+    return need + (size_t(1) << 30) < free_b;
+}
+
 // The single-pass fused functor.  `strategy` is the reference's
 // kmeans.fused.strategy ("feature_sum" -> FusedFeatureSum,
 // fused_feature_sum.hpp:191-444; "cluster_merge" -> FusedClusterMerge,

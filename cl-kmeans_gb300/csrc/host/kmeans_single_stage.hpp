@@ -161,18 +161,7 @@ private:
     }
 
     bool use_spatial_order(size_t d, size_t n, size_t k) const {
-        if (spatial_mode_ < 0) return false;
-        if (!(std::is_same<PointT, float>::value && std::is_same<LabelT, uint32_t>::value &&
-              std::is_same<MassT, uint32_t>::value && ColMajor))
-            return false;
-        if (d < 1 || d > 8 || k > 32 || n == 0 || n > 0xffffffffull) return false;
-        if (spatial_mode_ > 0) return true;
-        if (n < (1ull << 20) || this->max_iterations < 8) return false;
-        size_t free_b = 0, total_b = 0;
-        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
-        const size_t need = n * d * sizeof(PointT) + n * 2 * sizeof(LabelT) +
-                            ckm_spatial_sort_workspace_bytes(n, (uint32_t)d);
-        return need + (size_t(1) << 30) < free_b;
+        return spatial_order_eligible<PointT, LabelT, MassT, ColMajor>(spatial_mode_, d, n, k, this->max_iterations);
     }
 
     FusedLloyd<PointT, LabelT, MassT> engine_;

@@ -59,12 +59,48 @@ public:
         Event cu_done;
         this->reset_progress();
         if (this->converge) prev_.resize(k * d);
+        // spatial order (as in the single-stage strategy): labeling and
+        // centroid update run on a Z-ordered copy, the labeling box-pruned;
+        // the last iteration of a full run uses the caller's order
+        const bool spatial =
+            spatial_order_eligible<PointT, LabelT, MassT, ColMajor>(spatial_mode_, d, n, k, this->max_iterations);
+        if (spatial) {
+            auto& dp = this->measurement->add_datapoint().set_name("SpatialSort");
+            Event& ev = dp.add_event(q_labeling);
+            sorted_points_.resize(n * d);
+            perm_.resize(n);
+            sort_ws_.resize(ckm_spatial_sort_workspace_bytes(n, (uint32_t)d));
+            ckm_check(ckm_spatial_sort_f32((uint32_t)d, n, reinterpret_cast<const float*>(points_.data()),
+                                           reinterpret_cast<float*>(sorted_points_.data()), perm_.data(),
+                                           sort_ws_.data(), sort_ws_.size(), q_labeling.get()),
+                      "SpatialSort");
+            ev.record_end(q_labeling);
+            cu_done = ev;
+        }
+        bool labels_sorted = false;
         for (uint32_t it = 0; it < this->max_iterations; ++it) {
             WaitList ll_wait;
             ll_wait.insert(cu_done);
-            Event ll = f_labeling(q_labeling, d, n, k, points_.begin(), points_.end(), centroids_.begin(),
-                                  centroids_.end(), labels_.begin(), labels_.end(),
-                                  this->measurement->add_datapoint((int)it), ll_wait);
+            const bool sorted_it = spatial && it + 1 < this->max_iterations;
+            labels_sorted = sorted_it;
+            const PointT* it_points = sorted_it ? sorted_points_.data() : points_.data();
+            Event ll;
+            if (sorted_it) {
+                ll_wait.enqueue_wait(q_labeling);
+                auto& dp = this->measurement->add_datapoint((int)it).set_name("LabelingSorted");
+                Event& ev = dp.add_event(q_labeling);
+                ckm_check(ckm_labeling_sorted_f32((uint32_t)d, n, (uint32_t)k,
+                                                  reinterpret_cast<const float*>(it_points),
+                                                  reinterpret_cast<const float*>(centroids_.data()),
+                                                  reinterpret_cast<uint32_t*>(labels_.data()), q_labeling.get()),
+                          "LabelingSorted");
+                ev.record_end(q_labeling);
+                ll = ev;
+            } else {
+                ll = f_labeling(q_labeling, d, n, k, points_.begin(), points_.end(), centroids_.begin(),
+                                centroids_.end(), labels_.begin(), labels_.end(),
+                                this->measurement->add_datapoint((int)it), ll_wait);
+            }
             WaitList after_ll{ll};
             after_ll.enqueue_wait(q_mass_update);
             masses_.fill_zero_async(q_mass_update);
@@ -72,7 +108,7 @@ public:
                                      masses_.end(), this->measurement->add_datapoint((int)it), after_ll);
             WaitList cu_wait{ll, mu};
             // Sums go to FP64 scratch (DEFER); the divide reads them there.
-            Event cu = cu_engine_.launch(q_centroid_update, d, n, k, points_.data(), centroids_.data(),
+            Event cu = cu_engine_.launch(q_centroid_update, d, n, k, it_points, centroids_.data(),
                                          labels_.data(), masses_.data(), CKM_MODE_DEFER,
                                          this->measurement->add_datapoint((int)it), cu_wait);
             if (this->converge)  // the divide below overwrites the centroids in place
@@ -92,6 +128,17 @@ public:
                                       q_centroid_update))
                 break;
         }
+        if (labels_sorted) {
+            // stopped early on the convergence test: labels back to the
+            // caller's order
+            q_labeling.finish();
+            q_mass_update.finish();
+            q_centroid_update.finish();
+            labels_out_.resize(n);
+            ckm_check(ckm_unpermute_u32(n, perm_.data(), reinterpret_cast<const uint32_t*>(labels_.data()),
+                                        reinterpret_cast<uint32_t*>(labels_out_.data()), q_centroid_update.get()),
+                      "UnpermuteLabels");
+        }
         q_labeling.finish();
         q_mass_update.finish();
         q_centroid_update.finish();
@@ -100,7 +147,7 @@ public:
         last_total_ns_ = total_time;
 
         download("CentroidsD2H", centroids_, this->io_centroids(), k * d);
-        download("LabelsD2H", labels_, this->out_labels(), n);
+        download("LabelsD2H", labels_sorted ? labels_out_ : labels_, this->out_labels(), n);
         download("MassesD2H", masses_, this->out_masses(), k);
         q_centroid_update.finish();
         h2d_bytes_ = (n * d + k * d) * sizeof(PointT);
@@ -123,6 +170,9 @@ public:
     void set_labeling_queue(Stream q) { q_labeling = q; record_device("Labeling", q); }
     void set_mass_update_queue(Stream q) { q_mass_update = q; record_device("MassUpdate", q); }
     void set_centroid_update_queue(Stream q) { q_centroid_update = q; record_device("CentroidUpdate", q); }
+
+    // Spatial order of the iterations (see spatial_order_eligible).
+    void set_spatial_order(int mode) { spatial_mode_ = mode; }
 
     uint64_t last_total_ns() const { return last_total_ns_; }
     uint64_t h2d_bytes() const { return h2d_bytes_; }
@@ -152,8 +202,12 @@ private:
     Stream q_labeling, q_mass_update, q_centroid_update;
     DeviceVector<PointT> points_, centroids_, prev_;
     ConvergenceProbe<PointT, LabelT, MassT> probe_;
-    DeviceVector<LabelT> labels_;
+    DeviceVector<LabelT> labels_, labels_out_;
     DeviceVector<MassT> masses_;
+    DeviceVector<PointT> sorted_points_;
+    DeviceVector<uint32_t> perm_;
+    DeviceVector<unsigned char> sort_ws_;
+    int spatial_mode_ = 0;
     uint64_t last_total_ns_ = 0, h2d_bytes_ = 0, d2h_bytes_ = 0;
 };
 

@@ -75,6 +75,7 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
             s.set_centroid_updater(cc);
             s.set_converge(cfg->converge != 0);
             s.set_tolerance(cfg->tolerance);
+            s.set_spatial_order(cfg->spatial_order);
             s.run_raw(iters, d, n, k, points, centroids, masses, labels);
             done = (uint32_t)s.iterations_done();
             conv = s.did_converge() ? 1u : 0u;

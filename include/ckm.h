@@ -125,6 +125,9 @@ int ckm_fused_sorted_f32(uint32_t num_features, uint64_t num_points, uint32_t nu
                          const float *points, const float *old_centroids, float *new_centroids,
                          uint32_t *labels, uint32_t *masses, void *scratch, size_t scratch_bytes,
                          int mode, ckm_stream_t stream);
+/* ckm_labeling_f32 with the same per-warp box pruning (labels unchanged). */
+int ckm_labeling_sorted_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
+                            const float *points, const float *centroids, uint32_t *labels, ckm_stream_t stream);
 int ckm_unpermute_u32(uint64_t num_points, const uint32_t *perm, const uint32_t *in, uint32_t *out,
                       ckm_stream_t stream);
 

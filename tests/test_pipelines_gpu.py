@@ -132,14 +132,27 @@ def test_single_stage_spatial_order(ckm, oracle, cuda, n, d, k, iters, mode):
     _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L.view(np.uint32))
 
 
-def test_single_stage_spatial_order_converging(ckm, oracle, cuda):
+@pytest.mark.parametrize("n,d,k,iters,mode", [(100003, 4, 10, 10, 1), (1 << 20, 4, 16, 9, 0), (50001, 8, 32, 8, 1)])
+def test_three_stage_spatial_order(ckm, oracle, cuda, n, d, k, iters, mode):
+    """three_stage with the spatial order: box-pruned labeling and the
+    centroid update on the sorted copy, last iteration in the caller's
+    order; results as the oracle's."""
+    P = blobs(n, d, k, seed=3 * n + k)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    C, M, L, info = ckm.kmeans_run(P, d, k, iters, C0, pipeline="three_stage", spatial_order=mode)
+    assert info.iterations == iters
+    _e2e_check(oracle, P, n, d, k, iters, C0, C, M, L.view(np.uint32))
+
+
+@pytest.mark.parametrize("pipeline", ["single_stage", "three_stage"])
+def test_spatial_order_converging(ckm, oracle, cuda, pipeline):
     """A spatial-order run that stops on the convergence test before the
     iteration cap ends on the sorted set; its labels are mapped back to the
     caller's order and equal the oracle's for that many iterations."""
     n, d, k = 100003, 4, 10
     P = blobs(n, d, k, seed=5)
     C0 = oracle.first_x_f32(P, n, d, k)
-    C, M, L, info = ckm.kmeans_run(P, d, k, 60, C0, pipeline="single_stage", spatial_order=1, converge=True,
+    C, M, L, info = ckm.kmeans_run(P, d, k, 60, C0, pipeline=pipeline, spatial_order=1, converge=True,
                                    tolerance=1e-4)
     assert info.converged == 1 and info.iterations < 60
     _e2e_check(oracle, P, n, d, k, int(info.iterations), C0, C, M, L.view(np.uint32))
