@@ -310,6 +310,7 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
             s->set_centroid_updater(cu);
             s->set_converge(km.converge);
             s->set_tolerance(gb.tolerance);
+            s->set_spatial_order(gb.spatial_order);
             kmeans = [s](size_t a, size_t b, std::shared_ptr<const std::vector<P>> c, std::shared_ptr<std::vector<P>> e,
                          std::shared_ptr<std::vector<M>> f, std::shared_ptr<std::vector<L>> g) {
                 return (*s)(a, b, c, e, f, g);
@@ -344,6 +345,7 @@ int run_bench(const CmdOptions& opt, const ConfigurationParser& config) {
             s->set_fused(fu);
             s->set_converge(km.converge);
             s->set_tolerance(gb.tolerance);
+            s->set_spatial_order(gb.spatial_order);
             kmeans = [s](size_t a, size_t b, std::shared_ptr<const std::vector<P>> c, std::shared_ptr<std::vector<P>> e,
                          std::shared_ptr<std::vector<M>> f, std::shared_ptr<std::vector<L>> g) {
                 return (*s)(a, b, c, e, f, g);
@@ -471,7 +473,9 @@ int print_config(const ConfigurationParser& c) {
     std::cout << "kmeans.fused.vector_length=" << f.vector_length << "\n";
     std::cout << "kmeans.gb300.device_budget_mib=" << g.device_budget_mib << "\nkmeans.gb300.chunk_mib=" << g.chunk_mib
               << "\nkmeans.gb300.copy_streams=" << g.copy_streams << "\nkmeans.gb300.graphs=" << g.graphs
-              << "\nkmeans.gb300.tolerance=" << g.tolerance << "\n";
+              << "\nkmeans.gb300.tolerance=" << g.tolerance
+              << "\nkmeans.gb300.spatial_order=" << (g.spatial_order > 0 ? "on" : (g.spatial_order < 0 ? "off" : "auto"))
+              << "\n";
     return 1;
 }
 

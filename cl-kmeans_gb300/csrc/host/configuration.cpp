@@ -44,6 +44,7 @@ const std::map<std::string, Kind>& known_keys() {
         m["kmeans.gb300.copy_streams"] = Kind::Size;
         m["kmeans.gb300.graphs"] = Kind::Bool;
         m["kmeans.gb300.tolerance"] = Kind::String;  // a positive real, checked by to_real
+        m["kmeans.gb300.spatial_order"] = Kind::String;  // auto | on | off
         return m;
     }();
     return keys;
@@ -243,6 +244,12 @@ Gb300Configuration ConfigurationParser::get_gb300_configuration() const {
         else if (o.first == "kmeans.gb300.copy_streams") c.copy_streams = to_size(o.first, v);
         else if (o.first == "kmeans.gb300.graphs") c.graphs = to_bool(o.first, v);
         else if (o.first == "kmeans.gb300.tolerance") c.tolerance = to_real(o.first, v);
+        else if (o.first == "kmeans.gb300.spatial_order") {
+            if (v == "auto") c.spatial_order = 0;
+            else if (v == "on") c.spatial_order = 1;
+            else if (v == "off") c.spatial_order = -1;
+            else throw std::invalid_argument("kmeans.gb300.spatial_order must be auto, on or off, not '" + v + "'");
+        }
     }
     return c;
 }

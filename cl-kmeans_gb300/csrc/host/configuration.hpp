@@ -76,6 +76,8 @@ struct Gb300Configuration {
     size_t copy_streams = 2;       // buffered pipelines: host<->device copy streams
     bool graphs = true;            // capture the iteration loop in a CUDA graph where possible
     double tolerance = 1e-4;       // kmeans.converge: stop below this relative centroid shift
+    int spatial_order = 0;         // single / three stage: iterate on a spatially ordered copy
+                                   // ("auto" = 0, "on" = 1, "off" = -1)
 };
 
 class ConfigurationParser {

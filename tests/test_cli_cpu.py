@@ -147,3 +147,14 @@ def test_converge_and_tolerance_keys(ckm, tmp_path):
     for bad in ("0", "-1e-3", "abc"):
         with pytest.raises(ValueError):
             parse(ckm, tmp_path, base + "[kmeans.gb300]\ntolerance = %s\n" % bad)
+
+
+def test_spatial_order_key(ckm, tmp_path):
+    """[kmeans.gb300] spatial_order = auto | on | off (default auto)."""
+    base = "[kmeans]\nclusters = 4\npipeline = single_stage\niterations = 10\n"
+    assert parse(ckm, tmp_path, base)["kmeans.gb300.spatial_order"] == "auto"
+    for v in ("on", "off", "auto"):
+        c = parse(ckm, tmp_path, base + "[kmeans.gb300]\nspatial_order = %s\n" % v)
+        assert c["kmeans.gb300.spatial_order"] == v
+    with pytest.raises(ValueError):
+        parse(ckm, tmp_path, base + "[kmeans.gb300]\nspatial_order = sometimes\n")
