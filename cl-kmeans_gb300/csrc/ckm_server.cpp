@@ -97,11 +97,11 @@ struct ckm_server {
     std::vector<ckm_server_result> results;
     uint64_t submitted = 0, completed = 0;
     bool stop = false;
-    std::thread small_thread, large_thread;
+    std::thread small_thread, large_thread, retire_thread;
     // device
     cudaMemPool_t pool = nullptr;
-    cudaStream_t s_up = nullptr, s_comp = nullptr, s_large = nullptr;
-    cudaEvent_t ev_up = nullptr;
+    cudaStream_t s_up = nullptr, s_comp = nullptr, s_large = nullptr, s_down = nullptr;
+    cudaEvent_t ev_up = nullptr, ev_status = nullptr;
     BatchStatus* d_status = nullptr;   // [SLOTS]
     unsigned int* d_tickets = nullptr; // [SLOTS]
     BatchStatus* h_status = nullptr;   // pinned copy
@@ -109,6 +109,19 @@ struct ckm_server {
     ::ckm_batch* batch = nullptr;
     cudaEvent_t ev_s0 = nullptr, ev_s1 = nullptr;
     ckm_server_stats stats{};  // written by the batched lane under mu
+    // finished jobs of the batched lane, handed to the retire thread: their
+    // results are copied out after the round's event, then they are released
+    struct Retiring {
+        cudaEvent_t ev;              // recorded on s_comp after the round
+        std::vector<SJob*> jobs;
+        std::vector<BatchStatus> status;
+    };
+    std::mutex rmu;
+    std::condition_variable cv_retire;
+    std::deque<Retiring> retire_q;
+    std::vector<cudaEvent_t> free_events;
+    bool retire_stop = false;
+    uint64_t retiring_jobs = 0;      // queued or being copied out (under rmu)
 };
 
 namespace {
@@ -185,45 +198,117 @@ void release_small(ckm_server* S, SJob* j, cudaStream_t s) {
     j->slot = -1;
 }
 
+// Takes queued jobs that fit the budget and the free slots and issues their
+// uploads on s_up; they join the next round.
+void take_and_admit(ckm_server* S, std::vector<SJob*>& pending, uint64_t& admit_ns, uint64_t& admitted) {
+    std::vector<SJob*> take;
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        while (!S->small_q.empty() && !S->free_slots.empty()) {
+            SJob* j = S->small_q.front();
+            if (!charge(S, j->bytes)) break;  // waits until retirements free memory
+            S->small_q.pop_front();
+            j->slot = S->free_slots.back();
+            S->free_slots.pop_back();
+            take.push_back(j);
+        }
+    }
+    if (take.empty()) return;
+    const auto t0 = Clock::now();
+    for (SJob* j : take) {
+        const int st = admit_small(S, j);
+        if (st) {
+            release_small(S, j, S->s_up);
+            finish(S, j, st, 0, 0, 0.f, 0);
+        } else {
+            pending.push_back(j);
+        }
+    }
+    admit_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
+    admitted += take.size();
+}
+
+// The retire thread: for each batch of finished jobs, waits for the round
+// (its event), copies every job's centroids, masses and labels to the
+// caller's host arrays (pageable copies block this thread, not the lane),
+// then releases the jobs' memory and slots and posts their results.
+void retire_loop(ckm_server* S) {
+    cudaSetDevice(S->device);
+    const float tol = S->opt.tolerance;
+    for (;;) {
+        ckm_server::Retiring r;
+        {
+            std::unique_lock<std::mutex> lk(S->rmu);
+            S->cv_retire.wait(lk, [&] { return S->retire_stop || !S->retire_q.empty(); });
+            if (S->retire_q.empty()) break;  // stop requested and nothing left
+            r = std::move(S->retire_q.front());
+            S->retire_q.pop_front();
+        }
+        cudaError_t e = cudaStreamWaitEvent(S->s_down, r.ev, 0);
+        for (size_t i = 0; i < r.jobs.size() && e == cudaSuccess; ++i) {
+            SJob* j = r.jobs[i];
+            const BatchStatus& b = r.status[i];
+            const size_t kd = (size_t)j->u.num_clusters * j->u.num_features;
+            e = cudaMemcpyAsync(j->u.centroids, j->d_cent[b.parity & 1u], kd * 4, cudaMemcpyDeviceToHost, S->s_down);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(j->u.masses, j->d_masses, (size_t)j->u.num_clusters * 4, cudaMemcpyDeviceToHost,
+                                    S->s_down);
+            if (e == cudaSuccess && j->u.labels && j->u.num_points)
+                e = cudaMemcpyAsync(j->u.labels, j->d_labels, (size_t)j->u.num_points * 4, cudaMemcpyDeviceToHost,
+                                    S->s_down);
+        }
+        const cudaError_t es = cudaStreamSynchronize(S->s_down);
+        if (e == cudaSuccess) e = es;
+        for (size_t i = 0; i < r.jobs.size(); ++i) {
+            SJob* j = r.jobs[i];
+            const BatchStatus& b = r.status[i];
+            release_small(S, j, S->s_down);
+            finish(S, j, e == cudaSuccess ? CKM_OK : cuda_fail(e, "server: results"), b.iterations,
+                   (tol > 0.f && b.shift < tol) ? 1u : 0u, b.shift, 0);
+        }
+        {
+            std::lock_guard<std::mutex> g(S->rmu);
+            S->free_events.push_back(r.ev);
+            S->retiring_jobs -= r.jobs.size();
+        }
+        S->cv_work.notify_all();  // memory and slots are free again
+    }
+}
+
+uint64_t retiring_count(ckm_server* S) {
+    std::lock_guard<std::mutex> g(S->rmu);
+    return S->retiring_jobs;
+}
+
+// The batched lane.  A round: the admitted jobs become the batch's table,
+// `round_iterations` launches advance them, the status comes back.  The host
+// work around a round overlaps the GPU: the next jobs' uploads are issued
+// while the round runs, and the finished jobs go to the retire thread, which
+// copies their results out on its own stream while the next round runs.
 void small_lane(ckm_server* S) {
     cudaSetDevice(S->device);
     const float tol = S->opt.tolerance;
     const uint32_t max_it = S->opt.max_iterations, rounds = S->opt.round_iterations;
-    std::vector<SJob*> active;
+    std::vector<SJob*> active, pending;
     std::vector<BatchJobDev> dev;
     for (;;) {
-        std::vector<SJob*> admit;
-        {
+        uint64_t admit_ns = 0, admitted = 0;
+        take_and_admit(S, pending, admit_ns, admitted);
+        if (active.empty() && pending.empty()) {
             std::unique_lock<std::mutex> lk(S->mu);
-            if (active.empty())
-                S->cv_work.wait_for(lk, std::chrono::milliseconds(10),
-                                    [&] { return S->stop || !S->small_q.empty(); });
-            if (S->stop && S->small_q.empty() && active.empty()) break;
-            while (!S->small_q.empty() && !S->free_slots.empty()) {
-                SJob* j = S->small_q.front();
-                if (!charge(S, j->bytes)) break;  // waits until retirements free memory
-                S->small_q.pop_front();
-                j->slot = S->free_slots.back();
-                S->free_slots.pop_back();
-                admit.push_back(j);
-            }
+            if (S->stop && S->small_q.empty() && retiring_count(S) == 0) break;
+            if (S->small_q.empty())
+                S->cv_work.wait_for(lk, std::chrono::milliseconds(10), [&] { return S->stop || !S->small_q.empty(); });
+            else  // queued jobs wait for retirements to free memory or slots
+                S->cv_work.wait_for(lk, std::chrono::milliseconds(1));
+            continue;
         }
-        const auto t_admit = Clock::now();
-        for (SJob* j : admit) {
-            const int st = admit_small(S, j);
-            if (st) {
-                release_small(S, j, S->s_up);
-                finish(S, j, st, 0, 0, 0.f, 0);
-            } else {
-                active.push_back(j);
-            }
-        }
-        if (!admit.empty()) {
+        if (!pending.empty()) {
             cudaEventRecord(S->ev_up, S->s_up);
             cudaStreamWaitEvent(S->s_comp, S->ev_up, 0);
+            active.insert(active.end(), pending.begin(), pending.end());
+            pending.clear();
         }
-        const uint64_t admit_ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t_admit).count();
-        if (active.empty()) continue;
         const auto t_round = Clock::now();
 
         // one round over every admitted job
@@ -258,7 +343,10 @@ void small_lane(ckm_server* S) {
         if (st == CKM_OK) {
             e = cudaMemcpyAsync(S->h_status, S->d_status, (size_t)(max_slot + 1) * sizeof(BatchStatus),
                                 cudaMemcpyDeviceToHost, S->s_comp);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(S->s_comp);
+            if (e == cudaSuccess) e = cudaEventRecord(S->ev_status, S->s_comp);
+            // while the round runs: the next jobs' uploads
+            take_and_admit(S, pending, admit_ns, admitted);
+            if (e == cudaSuccess) e = cudaEventSynchronize(S->ev_status);
             if (e != cudaSuccess) st = cuda_fail(e, "server: status read-back");
         }
         if (st != CKM_OK) {  // the round failed: its jobs fail with the reason
@@ -273,32 +361,39 @@ void small_lane(ckm_server* S) {
         float steps_ms = 0.f;
         cudaEventElapsedTime(&steps_ms, S->ev_s0, S->ev_s1);
         const auto t_retire = Clock::now();
-        // retire the jobs that stopped in this round
-        std::vector<SJob*> keep, done;
+        // the jobs that stopped in this round go to the retire thread
+        std::vector<SJob*> keep;
+        ckm_server::Retiring r;
         for (SJob* j : active) {
             const BatchStatus& b = S->h_status[j->slot];
             if (!(b.flags & 2u)) {
                 keep.push_back(j);
                 continue;
             }
-            const size_t kd = (size_t)j->u.num_clusters * j->u.num_features;
-            e = cudaMemcpyAsync(j->u.centroids, j->d_cent[b.parity & 1u], kd * 4, cudaMemcpyDeviceToHost, S->s_comp);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(j->u.masses, j->d_masses, (size_t)j->u.num_clusters * 4, cudaMemcpyDeviceToHost,
-                                    S->s_comp);
-            if (e == cudaSuccess && j->u.labels && j->u.num_points)
-                e = cudaMemcpyAsync(j->u.labels, j->d_labels, (size_t)j->u.num_points * 4, cudaMemcpyDeviceToHost,
-                                    S->s_comp);
-            done.push_back(j);
+            r.jobs.push_back(j);
+            r.status.push_back(b);
         }
-        const cudaError_t es = cudaStreamSynchronize(S->s_comp);
-        if (e == cudaSuccess) e = es;
-        for (SJob* j : done) {
-            const BatchStatus b = S->h_status[j->slot];
-            release_small(S, j, S->s_comp);
-            finish(S, j, e == cudaSuccess ? CKM_OK : cuda_fail(e, "server: results"), b.iterations,
-                   (tol > 0.f && b.shift < tol) ? 1u : 0u, b.shift, 0);
+        if (!r.jobs.empty()) {
+            cudaEvent_t ev = nullptr;
+            {
+                std::lock_guard<std::mutex> g(S->rmu);
+                if (!S->free_events.empty()) {
+                    ev = S->free_events.back();
+                    S->free_events.pop_back();
+                }
+            }
+            if (!ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            r.ev = ev;
+            // the results are final once the round's kernels are done
+            cudaEventRecord(r.ev, S->s_comp);
+            {
+                std::lock_guard<std::mutex> g(S->rmu);
+                S->retiring_jobs += r.jobs.size();
+                S->retire_q.push_back(std::move(r));
+            }
+            S->cv_retire.notify_one();
         }
+        const size_t ndone = active.size() - keep.size();
         const auto t_end = Clock::now();
         {
             std::lock_guard<std::mutex> g(S->mu);
@@ -309,8 +404,8 @@ void small_lane(ckm_server* S) {
             x.steps_gpu_ns += (uint64_t)(steps_ms * 1e6);
             x.admit_ns += admit_ns;
             x.retire_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t_end - t_retire).count();
-            x.jobs_admitted += admit.size();
-            x.jobs_completed += done.size();
+            x.jobs_admitted += admitted;
+            x.jobs_completed += ndone;
         }
         active.swap(keep);
     }
@@ -471,7 +566,9 @@ int ckm_server_create(const ckm_server_options* options, ckm_server** out) {
     if ((e = cudaStreamCreateWithFlags(&S->s_up, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S->s_comp, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S->s_large, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&S->s_down, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&S->ev_up, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&S->ev_status, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreate(&S->ev_s0)) != cudaSuccess || (e = cudaEventCreate(&S->ev_s1)) != cudaSuccess)
         return cuda_fail(e, "server: streams");
     if ((e = cudaMalloc(&S->d_status, SLOTS * sizeof(BatchStatus))) != cudaSuccess ||
@@ -483,6 +580,7 @@ int ckm_server_create(const ckm_server_options* options, ckm_server** out) {
     int st = batch_create_external(&S->batch);
     if (st) return st;
     ckm_server* raw = S.release();
+    raw->retire_thread = std::thread(retire_loop, raw);
     raw->small_thread = std::thread(small_lane, raw);
     raw->large_thread = std::thread(large_lane, raw);
     *out = raw;
@@ -554,6 +652,13 @@ int ckm_server_destroy(ckm_server* S) {
     S->cv_work.notify_all();
     if (S->small_thread.joinable()) S->small_thread.join();
     if (S->large_thread.joinable()) S->large_thread.join();
+    {
+        std::lock_guard<std::mutex> g(S->rmu);
+        S->retire_stop = true;
+    }
+    S->cv_retire.notify_all();
+    if (S->retire_thread.joinable()) S->retire_thread.join();
+    for (cudaEvent_t ev : S->free_events) cudaEventDestroy(ev);
     cudaSetDevice(S->device);
     cudaDeviceSynchronize();
     ckm_batch_destroy(S->batch);
@@ -561,11 +666,13 @@ int ckm_server_destroy(ckm_server* S) {
     cudaFree(S->d_tickets);
     cudaFreeHost(S->h_status);
     cudaEventDestroy(S->ev_up);
+    cudaEventDestroy(S->ev_status);
     cudaEventDestroy(S->ev_s0);
     cudaEventDestroy(S->ev_s1);
     cudaStreamDestroy(S->s_up);
     cudaStreamDestroy(S->s_comp);
     cudaStreamDestroy(S->s_large);
+    cudaStreamDestroy(S->s_down);
     if (S->pool) cudaMemPoolDestroy(S->pool);
     delete S;
     return CKM_OK;
