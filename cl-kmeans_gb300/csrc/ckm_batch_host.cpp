@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -39,6 +40,7 @@ struct ckm_batch {
     unsigned int* d_work = nullptr;        // segments claimed in the current step
     // schedule
     uint32_t grid = 0, tile = 1024, ctas_per_sm = 1, block = 512, flush = 16, segments = 0;
+    uint32_t use_umma = 0;                // d = 32 / 64 segments may use the tensor cores
     float tol = 0.f;                      // convergence stop (0: none)
     uint32_t max_it = 0;                  // iteration cap (0: none)
     uint32_t jobs_capacity = 0;           // entries of d_jobs
@@ -110,6 +112,16 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
     // one CTA per SM runs 512 threads (16 warps beside the whole shared
     // memory); two or more run 256 threads each
     const uint32_t block = ctas_per_sm <= 1 ? 512u : 256u;
+    // the tensor-core path (d = 32 / 64; 512-thread CTAs, one per SM, 256
+    // TMEM columns each) takes its operand tiles from the same budget, so a
+    // batch with such jobs gets all of it
+    bool umma_jobs = false;
+    for (const auto& j : b->jobs)
+        umma_jobs = umma_jobs || ((j.num_features == 32 || j.num_features == 64) &&
+                                  j.num_clusters >= UMMA_MIN_K && j.num_clusters <= UMMA_MAX_K);
+    const char* env = std::getenv("CKM_BATCH_UMMA");
+    const bool umma_on = umma_jobs && block == 512 && !(env && env[0] == '0');
+    if (umma_on) acc_cap = budget - cent_cap;
     int bps = 0;
     int st = batched_blocks_per_sm(cent_cap + acc_cap, block, &bps);
     if (st) return st;
@@ -139,6 +151,7 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
     b->segments = (uint32_t)segs.size();
     b->cent_cap = cent_cap;
     b->acc_cap = acc_cap;
+    b->use_umma = umma_on ? 1u : 0u;
     for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
     b->graphs.clear();
     return CKM_OK;
@@ -146,7 +159,7 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
 
 int step(ckm_batch* b, cudaStream_t s) {
     return launch_batched(b->d_jobs, b->d_segs, b->segments, b->d_work, b->tol, b->max_it, b->grid, b->block, b->tile,
-                          b->flush, b->cent_cap, b->acc_cap, s);
+                          b->flush, b->cent_cap, b->acc_cap, b->use_umma, s);
 }
 
 int autotune(ckm_batch* b, cudaStream_t s) {
@@ -364,10 +377,15 @@ int ckm_batch_status(ckm_batch* b, float* shifts, uint32_t* iterations, ckm_stre
                                     (cudaStream_t)stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "ckm_batch_status");
+    uint32_t failed = 0xffffffffu;
     for (uint32_t j = 0; j < b->num_jobs; ++j) {
         if (shifts) shifts[j] = st[j].shift;
         if (iterations) iterations[j] = st[j].iterations;
+        if ((st[j].flags & 4u) && failed == 0xffffffffu) failed = j;
     }
+    if (failed != 0xffffffffu)
+        return fail(CKM_ERR_CUDA, "batched: a wait for the tensor cores timed out (job " + std::to_string(failed) +
+                                      " failed and is skipped by later steps)");
     return CKM_OK;
 }
 

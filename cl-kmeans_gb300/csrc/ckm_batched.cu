@@ -27,6 +27,7 @@
 #include "ckm_device.cuh"
 #include "ckm_internal.h"
 #include "ckm_mma_screen.cuh"
+#include "ckm_umma_batch.cuh"
 
 namespace ckm {
 
@@ -262,9 +263,30 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
                                                      const BatchSegment* __restrict__ segs, uint32_t num_segs,
                                                      unsigned int* __restrict__ work, float tol, uint32_t max_it,
                                                      uint32_t tile,
-                                                     uint32_t flush_tiles, size_t cent_cap, size_t acc_cap) {
+                                                     uint32_t flush_tiles, size_t cent_cap, size_t acc_cap,
+                                                     uint32_t use_umma) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned int s_last, s_unit, s_cn_max;
+    // tensor-core path: TMEM accumulator, MMA-completion barrier, abort flag
+    __shared__ __align__(8) uint64_t s_ubar[2];  // one per CTA half
+    __shared__ uint32_t s_tmem;
+    __shared__ unsigned int s_abort;
+    const uint32_t ubar = umma::smem_u32(&s_ubar[0]);
+    const uint32_t ubase = (umma::smem_u32(smem) + 1023u) & ~1023u;
+    uint32_t uphase = 0;
+    bool aborted = false;
+    if (BT == 512 && use_umma) {
+        if (threadIdx.x == 0) {
+            umma::mbar_init(ubar, 1);
+            umma::mbar_init(ubar + 8u, 1);
+            umma::mbar_fence_init();
+            s_abort = 0u;
+        }
+        if (threadIdx.x < 32) umma::tmem_alloc(umma::smem_u32(&s_tmem), UMMA_TMEM_COLS);
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+    }
     for (;;) {
         // dynamic schedule: the next unclaimed segment (largest first)
         __syncthreads();  // every thread has read the previous s_unit and cm
@@ -284,10 +306,59 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
         if (st.flags & 1u) continue;  // job inactive this step
         const int parity = (int)(st.parity & 1u);
         const uint32_t k = J.k, d = J.d;
+        const size_t total = cent_cap + acc_cap;
+        // d = 32 / 64 on the tensor cores (tcgen05) when the segment's layout
+        // and a one-copy table fit, and the centroids are within fp16's range
+        bool umma = BT == 512 && use_umma && (d == 32 || d == 64) && k >= UMMA_MIN_K && k <= UMMA_MAX_K &&
+                    umma_region_bytes(k) + ((size_t)k * d + k) * sizeof(float) <= total;
+        if constexpr (BT == 512) if (umma) {
+            __shared__ UmmaScratch s_us;
+            const uint32_t kp = umma_k_pad(k);
+            const UmmaLayout L = umma_layout(kp);
+            const size_t table_off = umma_region_bytes(k);
+            const uint32_t copies = table_copies(k, d, total - table_off);
+            float* s_sum = reinterpret_cast<float*>(smem + table_off);
+            unsigned int* s_mass = reinterpret_cast<unsigned int*>(s_sum + (size_t)k * d * copies);
+            const float* C = cent_of(J, parity);
+            __syncthreads();  // previous segment's readers of shared memory are done
+            if (d == 32) umma_stage<32, BT>(C, k, ubase, L, kp, s_us.cn, &s_cn_max);
+            else umma_stage<64, BT>(C, k, ubase, L, kp, s_us.cn, &s_cn_max);
+            {
+                const size_t words = (size_t)k * d * copies + k;
+                for (size_t i = threadIdx.x; i < words; i += BT) s_sum[i] = 0.f;
+            }
+            umma::fence_proxy_async_smem();
+            __syncthreads();
+            const float cm = __uint_as_float(s_cn_max);
+            umma = cm < UMMA_MAX_ABS;  // same value in every thread
+            if (umma) {
+                for (uint32_t t = S.tile_begin; t < S.tile_end && !aborted; t += flush_tiles) {
+                    const uint32_t te = min(S.tile_end, t + flush_tiles);
+                    const bool ok = d == 32 ? run_tiles_umma<32>(J, C, t, te, tile, ubase, L, kp, s_tmem, ubar, uphase,
+                                                                 cm, s_sum, s_mass, copies, s_us, &s_abort)
+                                            : run_tiles_umma<64>(J, C, t, te, tile, ubase, L, kp, s_tmem, ubar, uphase,
+                                                                 cm, s_sum, s_mass, copies, s_us, &s_abort);
+                    if (!ok) {
+                        aborted = true;  // every thread: the flag was read after a barrier
+                        break;
+                    }
+                    if (copies) {
+                        __syncthreads();
+                        flush_tables<BT>(J, s_sum, s_mass, copies);
+                        __syncthreads();
+                    }
+                }
+                if (aborted) {
+                    // the job cannot finish this step: parked with the error bit
+                    if (threadIdx.x == 0) atomicOr(&J.status->flags, 7u);
+                    break;
+                }
+            }
+        }
+        if (!umma) {
         // shared memory of this segment: centroids (MMA fragments, or rows for
         // the SIMT screen / exact loop, or none) at the start, the sum table
         // in the rest
-        const size_t total = cent_cap + acc_cap;
         const bool mma = (d == 32 || d == 64) && k >= mma_min_k(d) &&
                          mma_cent_bytes(k, d) + ((size_t)k * d + k) * sizeof(float) <= total;
         const size_t cbytes = ((size_t)k * d + ((k + 3u) & ~3u)) * sizeof(float);  // rows + |c|^2
@@ -340,6 +411,7 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
                 __syncthreads();
             }
         }
+        }
         // ticket: the CTA that completes the job's tiles finalises it
         __threadfence();
         __syncthreads();
@@ -352,6 +424,15 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
         if (s_last) {
             __threadfence();
             finalize_job<BT>(J, parity, tol, max_it);
+        }
+    }
+    if (BT == 512 && use_umma) {
+        // (after an abort each half waited, bounded, for its last MMA)
+        umma::fence_before_sync();
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            umma::fence_after_sync();
+            umma::tmem_dealloc(s_tmem, UMMA_TMEM_COLS);
         }
     }
 }
@@ -378,7 +459,7 @@ int ensure_batched_attr() {
 template <int BT>
 int launch_batched_t(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
                      float tol, uint32_t max_it, uint32_t grid, uint32_t tile, uint32_t flush_tiles, size_t cent_cap,
-                     size_t acc_cap, cudaStream_t s) {
+                     size_t acc_cap, uint32_t use_umma, cudaStream_t s) {
     const size_t smem = cent_cap + acc_cap;
     int st = ensure_batched_attr<BT>();
     if (st) return st;
@@ -386,7 +467,7 @@ int launch_batched_t(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t
     cudaError_t e0 = cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
     if (e0 != cudaSuccess) return cuda_fail(e0, "batched work counter");
     batched_kernel<BT><<<grid, BT, smem, s>>>(jobs, segs, num_segs, work, tol, max_it, tile, flush_tiles, cent_cap,
-                                              acc_cap);
+                                              acc_cap, use_umma);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batched launch");
@@ -396,13 +477,13 @@ int launch_batched_t(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t
 
 int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
                    float tol, uint32_t max_it, uint32_t grid, uint32_t block, uint32_t tile, uint32_t flush_tiles,
-                   size_t cent_cap, size_t acc_cap, cudaStream_t s) {
+                   size_t cent_cap, size_t acc_cap, uint32_t use_umma, cudaStream_t s) {
     if (block == 512)
         return launch_batched_t<512>(jobs, segs, num_segs, work, tol, max_it, grid, tile, flush_tiles, cent_cap,
-                                     acc_cap, s);
+                                     acc_cap, use_umma, s);
     if (block != 256) return fail(CKM_ERR_INVALID_ARGUMENT, "batched: CTA size must be 256 or 512");
     return launch_batched_t<256>(jobs, segs, num_segs, work, tol, max_it, grid, tile, flush_tiles, cent_cap, acc_cap,
-                                 s);
+                                 use_umma, s);
 }
 
 int batched_blocks_per_sm(size_t smem, uint32_t block, int* out) {

@@ -263,8 +263,10 @@ void retire_loop(ckm_server* S) {
             SJob* j = r.jobs[i];
             const BatchStatus& b = r.status[i];
             release_small(S, j, S->s_down);
-            finish(S, j, e == cudaSuccess ? CKM_OK : cuda_fail(e, "server: results"), b.iterations,
-                   (tol > 0.f && b.shift < tol) ? 1u : 0u, b.shift, 0);
+            int st = e == cudaSuccess ? CKM_OK : cuda_fail(e, "server: results");
+            if (st == CKM_OK && (b.flags & 4u))
+                st = fail(CKM_ERR_CUDA, "server: a wait for the tensor cores timed out in the job's round");
+            finish(S, j, st, b.iterations, (tol > 0.f && b.shift < tol) ? 1u : 0u, b.shift, 0);
         }
         {
             std::lock_guard<std::mutex> g(S->rmu);

@@ -227,3 +227,81 @@ def test_batch_screen_fallback_offsets_and_huge_centroids(ckm, oracle, cuda):
             assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
     finally:
         b.close()
+
+
+UMMA_SHAPES = [(20000, 32, 16), (4099, 64, 17), (1000, 32, 31), (129, 64, 63), (128, 32, 64), (3000, 64, 65),
+               (5000, 32, 100), (2500, 64, 128), (100, 32, 200), (4500, 64, 255), (3333, 32, 256), (1, 64, 16),
+               (777, 64, 256), (9000, 32, 20)]
+
+
+@pytest.mark.parametrize("umma", ["1", "0"])
+def test_batch_tensor_core_path_lockstep(ckm, oracle, cuda, umma, monkeypatch):
+    """d = 32 / 64 jobs with 16 <= k <= 256 take the tcgen05 path in
+    512-thread CTAs (CKM_BATCH_UMMA=0 switches it off): k not a multiple of
+    the column groups, n not a multiple of 128 and below 128.  Labels stay the
+    oracle's bit for bit on both paths."""
+    import torch
+    monkeypatch.setenv("CKM_BATCH_UMMA", umma)
+    jobs, host = make_jobs(cuda, oracle, UMMA_SHAPES, seed=21)
+    b = ckm.Batch(jobs, tile_points=1024, ctas_per_sm=1)
+    try:
+        for it in range(3):
+            b.sync()
+            torch.cuda.synchronize()
+            Cin = [j["centroids"].cpu().numpy().copy() for j in jobs]
+            b.step()
+            b.sync()
+            torch.cuda.synchronize()
+            for j, P, C0 in zip(jobs, host, Cin):
+                n, d, k = j["n"], j["d"], j["k"]
+                lab = j["labels"][:n].cpu().numpy().view(np.uint32)
+                ref = oracle.label_f32(P, n, d, k, C0)
+                assert np.array_equal(lab, ref), (it, n, d, k, int((lab != ref).sum()))
+                assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+                check_centroids(oracle, P, n, d, k, ref, j["centroids"].cpu().numpy())
+        assert np.all(b.status()[1] == 3)
+    finally:
+        b.close()
+
+
+def test_batch_tensor_core_path_edge_values(ckm, oracle, cuda):
+    """On the tcgen05 path: exact ties, a NaN centroid, points with NaN or
+    infinite coordinates, points beyond fp16's range (|x| >= 2^15: the full
+    exact scan), points far from every centroid (many candidates) and
+    duplicated points.  Labels stay the oracle's."""
+    import torch
+    shapes = [(6000, 32, 40), (5000, 64, 64), (3000, 64, 200), (4000, 32, 17)]
+    jobs, host = make_jobs(cuda, oracle, shapes, seed=23)
+    for i, j in enumerate(jobs):
+        n, d, k = j["n"], j["d"], j["k"]
+        P = host[i].reshape(d, n).copy()
+        P[:, 50:400] = P[:, 50:51]              # duplicates
+        P[3, 500] = np.nan
+        P[0, 600] = np.inf
+        P[1, 700] = -np.inf
+        P[:, 800:900] += np.float32(40000.0)     # |x| >= 2^15
+        P[2, 950] = np.float32(70000.0)          # beyond fp16's largest finite value
+        P[:, 1000:1100] *= np.float32(300.0)     # far from every centroid
+        host[i] = np.ascontiguousarray(P).reshape(-1)
+        j["points"].copy_(torch.from_numpy(host[i]))
+        C = np.nan_to_num(oracle.first_x_f32(host[i], n, d, k), nan=0.0, posinf=1.0, neginf=-1.0).reshape(d, k)
+        C = np.clip(C, -100.0, 100.0)
+        C[:, 7] = C[:, 3]
+        C[:, k - 1] = C[:, 5]
+        C[:, 10] = np.nan
+        j["centroids"].copy_(torch.from_numpy(np.ascontiguousarray(C, dtype=np.float32).reshape(-1)))
+    b = ckm.Batch(jobs, tile_points=1024, ctas_per_sm=1)
+    try:
+        Cin = [j["centroids"].cpu().numpy().copy() for j in jobs]
+        b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        for j, P, C0 in zip(jobs, host, Cin):
+            n, d, k = j["n"], j["d"], j["k"]
+            lab = j["labels"][:n].cpu().numpy().view(np.uint32)
+            ref = oracle.label_f32(P, n, d, k, C0)
+            assert np.array_equal(lab, ref), (n, d, k, int((lab != ref).sum()), np.nonzero(lab != ref)[0][:10])
+            assert not np.any(lab == 7) and not np.any(lab == 10) and not np.any(lab == k - 1)
+            assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+    finally:
+        b.close()
