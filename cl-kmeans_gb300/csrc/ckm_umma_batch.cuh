@@ -148,10 +148,11 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t
 // x = hi + lo (+ residual): hi = fp16(x), lo = fp16(x - hi); x - hi is exact
 // in FP32.  Two values per 32-bit word, the lower feature in the low half.
 __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
-    const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
-    const __half la = __float2half_rn(a - __half2float(ha)), lb = __float2half_rn(b - __half2float(hb));
-    hi = (uint32_t)__half_as_ushort(ha) | ((uint32_t)__half_as_ushort(hb) << 16);
-    lo = (uint32_t)__half_as_ushort(la) | ((uint32_t)__half_as_ushort(lb) << 16);
+    const __half2 h = __floats2half2_rn(a, b);  // one packed conversion (a in the low half)
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // Eight consecutive features of row r as hi and lo chunks of the two tiles.
@@ -350,6 +351,13 @@ __device__ __forceinline__ bool run_tiles_umma(const BatchJobDev& J, const float
             umma::fence_proxy_async_smem();
             umma_detail::half_sync(half);
             if (PREF && b + 2 * UMMA_M < ce) load(b + 2 * UMMA_M);  // in flight during the MMA and the epilogue
+        if (!PREF && b + 2 * UMMA_M < ce) {
+            // d = 64: the next sub-tile's rows into L2 (feature th / 4, 32
+            // points from 32 (th % 4)), so its loads do not wait for HBM
+            const uint64_t pn = b + 2 * UMMA_M + (th & 3u) * 32u;
+            if (pn < ce)
+                asm volatile("prefetch.L2 [%0];" ::"l"(P + (size_t)(th >> 2) * n + pn) : "memory");
+        }
             if (th == 0) {
                 *s_need = 0u;
                 umma::fence_after_sync();
