@@ -30,6 +30,7 @@ STATUS = {
 # Every symbol include/ckm.h declares (checked by the tests).
 EXPORTS = [
     "ckm_status_string", "ckm_last_error", "ckm_version", "ckm_device_count", "ckm_launch_count",
+    "ckm_release_cached_memory",
     "ckm_scratch_bytes", "ckm_scratch_init",
     "ckm_fused_f32", "ckm_fused_f64", "ckm_fused_f32_noalloc", "ckm_labeling_f32", "ckm_labeling_f64",
     "ckm_mass_update_u32", "ckm_mass_update_u64", "ckm_centroid_update_f32", "ckm_centroid_update_f64",
@@ -108,6 +109,7 @@ def lib():
         "ckm_version": ([], i32),
         "ckm_device_count": ([ctypes.POINTER(ctypes.c_int)], i32),
         "ckm_launch_count": ([], u64),
+        "ckm_release_cached_memory": ([], i32),
         "ckm_scratch_bytes": ([u32, u32], sz),
         "ckm_scratch_init": ([vp, sz, vp], i32),
         "ckm_fused_f32": ([u32, u64, u32, vp, vp, vp, vp, vp, vp, sz, i32, vp], i32),

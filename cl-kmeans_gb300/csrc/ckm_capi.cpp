@@ -138,6 +138,16 @@ int ckm_device_count(int* count) {
 
 uint64_t ckm_launch_count(void) { return launch_count(); }
 
+int ckm_release_cached_memory(void) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    cudaMemPool_t pool = nullptr;
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    if (e == cudaSuccess) e = cudaMemPoolTrimTo(pool, 0);
+    return e == cudaSuccess ? CKM_OK : cuda_fail(e, "ckm_release_cached_memory");
+}
+
 size_t ckm_scratch_bytes(uint32_t num_features, uint32_t num_clusters) {
     return scratch_layout(num_features, num_clusters).total;
 }

@@ -10,6 +10,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -25,6 +26,37 @@ public:
 
 inline void cuda_check(cudaError_t e, const char* where) {
     if (e != cudaSuccess) throw CudaError(e, where);
+}
+
+// Device buffers of the strategies come from the current device's default
+// stream-ordered pool, set once per device to keep freed memory (no release
+// threshold): the multi-GiB buffers of one run are reused by the next instead
+// of being mapped and unmapped each time (a free of several GiB took tens of
+// milliseconds).  ckm_release_cached_memory() returns the cached memory.
+inline void* device_alloc(size_t bytes) {
+    static std::once_flag once[64];
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev >= 0 && dev < 64)
+        std::call_once(once[dev], [dev]() {
+            cudaMemPool_t pool = nullptr;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+                uint64_t keep = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+        });
+    void* p = nullptr;
+    cuda_check(cudaMallocAsync(&p, bytes, 0), "cudaMallocAsync");
+    // ready for every stream before the caller uses it
+    cuda_check(cudaStreamSynchronize(0), "cudaStreamSynchronize");
+    return p;
+}
+
+// The buffer may still be in use by work on any stream: the device finishes
+// first (as cudaFree would), then the memory goes back to the pool.
+inline void device_free(void* p) {
+    cudaDeviceSynchronize();
+    cudaFreeAsync(p, 0);
 }
 
 // A status from the C ABI that is not CKM_OK.
@@ -213,11 +245,7 @@ public:
     void resize(size_t n) {
         if (n == n_) return;
         release();
-        if (n) {
-            void* p = nullptr;
-            cuda_check(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
-            p_ = static_cast<T*>(p);
-        }
+        if (n) p_ = static_cast<T*>(device_alloc(n * sizeof(T)));
         n_ = n;
     }
     size_t size() const { return n_; }
@@ -240,7 +268,7 @@ public:
 
 private:
     void release() {
-        if (p_) cudaFree(p_);
+        if (p_) device_free(p_);
         p_ = nullptr;
         n_ = 0;
     }

@@ -76,6 +76,11 @@ int ckm_version(void);
 int ckm_device_count(int *count);
 /* Kernels this library has launched in this process (all threads). */
 uint64_t ckm_launch_count(void);
+/* The C++ strategies (ckm_kmeans_run_f32 / _f64 and the bench) take their
+ * device buffers from the current device's default stream-ordered pool and
+ * keep freed memory there for the next run.  This waits for the device and
+ * returns that cached memory to the system. */
+int ckm_release_cached_memory(void);
 
 /* ---------------------------------------------------------------------- */
 /* Scratch.  The fused, centroid-update and finalize calls merge per-CTA   */

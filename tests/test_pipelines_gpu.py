@@ -269,3 +269,19 @@ def test_centroid_shift_matches_numpy(ckm, cuda):
     assert L.ckm_centroid_shift_f32(d, k, dO.data_ptr(), dN.data_ptr(), out.data_ptr(), s.cuda_stream) == 0
     torch.cuda.synchronize()
     assert abs(float(out.item()) - want) <= 1e-6 * want
+
+
+def test_release_cached_memory_after_runs(ckm, oracle, cuda):
+    """The strategies keep their device buffers in the default stream-ordered
+    pool between runs; a second run of the same shape gives the same result,
+    and ckm_release_cached_memory returns the cached memory."""
+    n, d, k = 50000, 8, 12
+    P = blobs(n, d, 6, seed=5)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    outs = []
+    for _ in range(2):
+        C, M, L, _info = ckm.kmeans_run(P, d, k, 4, C0)
+        outs.append((C.copy(), M.copy(), L.copy()))
+    assert np.array_equal(outs[0][2], outs[1][2])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert ckm.lib().ckm_release_cached_memory() == 0
