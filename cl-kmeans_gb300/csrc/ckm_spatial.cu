@@ -257,72 +257,82 @@ __global__ void __launch_bounds__(SB) downsweep_kernel(const float* __restrict__
     uint16_t* s_src = reinterpret_cast<uint16_t*>(smem);                 // [chunk]
     unsigned char* s_din = reinterpret_cast<unsigned char*>(s_src + chunk);  // digit of local item j
     unsigned char* s_dig = s_din + chunk;                                 // digit at sorted position
-    __shared__ uint32_t s_hist[RADIX], s_off[RADIX], s_run[RADIX], s_wcnt[SB / 32][RADIX];
+    constexpr uint32_t NW = SB / 32;
+    // per warp and digit: the warp's count, then the absolute position of its
+    // next item of that digit
+    __shared__ uint32_t s_off[RADIX], s_wh[NW][RADIX], s_ws[NW];
     float lo[16], scale[16];
     load_range(ws, d, b, lo, scale);
     const uint64_t c = blockIdx.x;
     const uint64_t c0 = c * chunk;
     const uint32_t valid = (uint32_t)min((uint64_t)chunk, n - c0);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    // each warp owns a contiguous run of the chunk's items (chunk is a
+    // multiple of SB), so only warp-level synchronisation is needed while
+    // digits are counted and positions handed out; the warps' runs in order
+    // keep the sort stable
+    const uint32_t per = chunk / NW, w0 = warp * per;
 
-    // 1. digits and histogram
-    s_hist[threadIdx.x] = 0u;
-    s_run[threadIdx.x] = 0u;
-    __syncthreads();
-    for (uint32_t r = 0; r < chunk; r += SB) {
-        const uint32_t j = r + threadIdx.x;
+    // 1. digits and per-warp histograms
+    for (uint32_t t = lane; t < RADIX; t += 32) s_wh[warp][t] = 0u;
+    __syncwarp();
+    for (uint32_t r = 0; r < per; r += 32) {
+        const uint32_t j = w0 + r + lane;
         const bool ok = j < valid;
         const uint32_t active = __ballot_sync(0xffffffffu, ok);
         if (ok) {
             const uint32_t dg = item_digit(P, n, c0 + j, d, b, lo, scale, shift);
             s_din[j] = (unsigned char)dg;
             const uint32_t peers = __match_any_sync(active, dg);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_hist[dg], (uint32_t)__popc(peers));
+            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wh[warp][dg] += (uint32_t)__popc(peers);
         }
+        __syncwarp();
     }
-    __syncthreads();
-    // exclusive scan of the histogram (SB == RADIX: one digit per thread)
-    s_off[threadIdx.x] = s_hist[threadIdx.x];
-    __syncthreads();
-    for (uint32_t o = 1; o < RADIX; o <<= 1) {
-        const uint32_t y = threadIdx.x >= o ? s_off[threadIdx.x - o] : 0u;
-        __syncthreads();
-        s_off[threadIdx.x] += y;
-        __syncthreads();
-    }
-    s_off[threadIdx.x] -= s_hist[threadIdx.x];
     __syncthreads();
 
-    // 2. stable ranks
-    for (uint32_t r = 0; r < valid; r += SB) {
-        const uint32_t j = r + threadIdx.x;
+    // 2. thread t = digit t (SB == RADIX): the counts of the warps before each
+    // warp, the digit's total, and the exclusive scan of the totals
+    {
+        const uint32_t t = threadIdx.x;
+        uint32_t tot = 0;
+        for (uint32_t w = 0; w < NW; ++w) {
+            const uint32_t v = s_wh[w][t];
+            s_wh[w][t] = tot;
+            tot += v;
+        }
+        uint32_t incl = tot;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_ws[warp] = incl;
+        __syncthreads();
+        uint32_t base = 0;
+        for (uint32_t w = 0; w < warp; ++w) base += s_ws[w];
+        const uint32_t excl = base + incl - tot;
+        s_off[t] = excl;
+        for (uint32_t w = 0; w < NW; ++w) s_wh[w][t] += excl;
+    }
+    __syncthreads();
+
+    // 3. stable positions: each warp hands out positions to its items in order
+    for (uint32_t r = 0; r < per; r += 32) {
+        const uint32_t j = w0 + r + lane;
         const bool ok = j < valid;
         const uint32_t active = __ballot_sync(0xffffffffu, ok);
-        for (uint32_t t = lane; t < RADIX; t += 32) s_wcnt[warp][t] = 0u;
-        __syncwarp();  // the row is zero before any leader writes its count
-        uint32_t dg = 0, rank = 0;
         if (ok) {
-            dg = s_din[j];
+            const uint32_t dg = s_din[j];
             const uint32_t peers = __match_any_sync(active, dg);
-            rank = __popc(peers & ((1u << lane) - 1u));
-            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wcnt[warp][dg] = __popc(peers);
-        }
-        __syncthreads();
-        if (ok) {
-            uint32_t pre = s_run[dg];
-            for (uint32_t w = 0; w < warp; ++w) pre += s_wcnt[w][dg];
-            const uint32_t pos = s_off[dg] + pre + rank;
+            const uint32_t pos = s_wh[warp][dg] + (uint32_t)__popc(peers & ((1u << lane) - 1u));
             s_src[pos] = (uint16_t)j;
             s_dig[pos] = (unsigned char)dg;
+            __syncwarp(active);  // every lane has read its base before the leader moves it
+            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wh[warp][dg] += (uint32_t)__popc(peers);
         }
-        __syncthreads();
-        {
-            uint32_t add = 0;
-            for (uint32_t w = 0; w < SB / 32; ++w) add += s_wcnt[w][threadIdx.x];
-            s_run[threadIdx.x] += add;
-        }
-        __syncthreads();
+        __syncwarp();
     }
+    __syncthreads();
 
     // 3. write out
     for (uint32_t q = threadIdx.x; q < valid; q += SB) {
