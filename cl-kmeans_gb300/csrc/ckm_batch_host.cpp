@@ -151,7 +151,10 @@ int upload_schedule(ckm_batch* b, uint32_t tile, uint32_t ctas_per_sm, cudaStrea
     b->segments = (uint32_t)segs.size();
     b->cent_cap = cent_cap;
     b->acc_cap = acc_cap;
-    b->use_umma = umma_on ? 1u : 0u;
+    // CKM_BATCH_TEST_STALL=1 (tests only): the tensor-core waits run out, to
+    // check that a failed job is reported
+    const char* stall = std::getenv("CKM_BATCH_TEST_STALL");
+    b->use_umma = umma_on ? (1u | ((stall && stall[0] == '1') ? 2u : 0u)) : 0u;
     for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
     b->graphs.clear();
     return CKM_OK;

@@ -265,6 +265,9 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
                                                      uint32_t tile,
                                                      uint32_t flush_tiles, size_t cent_cap, size_t acc_cap,
                                                      uint32_t use_umma) {
+    // use_umma bit 0: the tcgen05 path may run; bit 1: failure-detection test
+    // (each CTA's first half gives up on its first tensor-core wait)
+    const bool umma_test_stall = (use_umma & 2u) != 0u;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned int s_last, s_unit, s_cn_max;
     // tensor-core path: TMEM accumulator, MMA-completion barrier, abort flag
@@ -335,9 +338,11 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
                 for (uint32_t t = S.tile_begin; t < S.tile_end && !aborted; t += flush_tiles) {
                     const uint32_t te = min(S.tile_end, t + flush_tiles);
                     const bool ok = d == 32 ? run_tiles_umma<32>(J, C, t, te, tile, ubase, L, kp, s_tmem, ubar, uphase,
-                                                                 cm, s_sum, s_mass, copies, s_us, &s_abort)
+                                                                 cm, s_sum, s_mass, copies, s_us, &s_abort,
+                                                                 umma_test_stall)
                                             : run_tiles_umma<64>(J, C, t, te, tile, ubase, L, kp, s_tmem, ubar, uphase,
-                                                                 cm, s_sum, s_mass, copies, s_us, &s_abort);
+                                                                 cm, s_sum, s_mass, copies, s_us, &s_abort,
+                                                                 umma_test_stall);
                     if (!ok) {
                         aborted = true;  // every thread: the flag was read after a barrier
                         break;

@@ -48,9 +48,10 @@ struct BatchSegment {
 // counter *work, which the launch resets to zero beforehand.  tol > 0 /
 // max_it > 0: a job whose shift falls below tol, or that has run max_it
 // iterations, parks itself (status flags bits 0 and 1).
-// block: threads per CTA, 256 or 512.  use_umma (512-thread CTAs, one per
-// SM): d = 32 / 64 segments may take the tensor-core path, each CTA holding
-// 256 TMEM columns.
+// block: threads per CTA, 256 or 512.  use_umma bit 0 (512-thread CTAs, one
+// per SM): d = 32 / 64 segments may take the tensor-core path, each CTA
+// holding 512 TMEM columns; bit 1: failure-detection test (the tensor-core
+// waits run out after 1 ms and the jobs are parked as failed).
 int launch_batched(const BatchJobDev* jobs, const BatchSegment* segs, uint32_t num_segs, unsigned int* work,
                    float tol, uint32_t max_it, uint32_t grid, uint32_t block, uint32_t tile, uint32_t flush_tiles,
                    size_t cent_cap, size_t acc_cap, uint32_t use_umma, cudaStream_t s);

@@ -126,13 +126,13 @@ __device__ __forceinline__ bool try_wait_hint(uint32_t bar, uint32_t parity, uin
 // Waits for the phase with a time limit; false when it did not complete.
 // One thread waits (the others are at a barrier), so it polls without a
 // suspend hint first: the MMAs of a sub-tile take about a microsecond.
-__device__ __forceinline__ bool wait_bounded(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool wait_bounded(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
     for (int i = 0; i < 4096; ++i)
         if (umma::mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = now_ns();
     for (;;) {
         if (try_wait_hint(bar, parity, 20000u)) return true;
-        if (now_ns() - t0 > UMMA_WAIT_NS) return false;
+        if (now_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -273,7 +273,7 @@ __device__ __forceinline__ bool run_tiles_umma(const BatchJobDev& J, const float
                                                uint32_t t1, uint32_t tile, uint32_t base, const UmmaLayout& L,
                                                uint32_t kp, uint32_t tmem, uint32_t bars, uint32_t& phase, float cm,
                                                float* s_sum, unsigned int* s_mass, uint32_t copies, UmmaScratch& us,
-                                               volatile unsigned int* s_abort) {
+                                               volatile unsigned int* s_abort, bool test_stall) {
     constexpr uint32_t G = 2;            // column groups per half
     constexpr int FPT = D / (int)G;      // features per thread
     static_assert(FPT % 8 == 0, "whole 16-byte chunks per thread");
@@ -305,6 +305,7 @@ __device__ __forceinline__ bool run_tiles_umma(const BatchJobDev& J, const float
     float* s_cut = us.cut + half * UMMA_M;
     volatile unsigned int* s_need = us.need + half;
     volatile unsigned int* my_abort = us.abort + half;
+    const unsigned long long wait_ns = test_stall ? 1000000ull : UMMA_WAIT_NS;
     const float* s_cn = us.cn;
     const float INF = __int_as_float(0x7f800000);
 
@@ -361,22 +362,26 @@ __device__ __forceinline__ bool run_tiles_umma(const BatchJobDev& J, const float
             if (th == 0) {
                 *s_need = 0u;
                 umma::fence_after_sync();
-                // the small cross products first, then x_h c_h (see the bound)
+                // failure-detection test (test_stall): the first half issues
+                // no MMA, so its wait below finds nothing and runs out (1 ms)
+                if (!(test_stall && half == 0)) {
+                    // the small cross products first, then x_h c_h (see the bound)
 #pragma unroll
-                for (uint32_t ks = 0; ks < (uint32_t)D / 16u; ++ks) {
-                    const uint64_t ah = umma::sw128_desc(sA + ks * 32u);
-                    const uint64_t al = umma::sw128_desc(sAl + ks * 32u);
-                    const uint64_t bh = umma::sw128_desc(base + L.bh + ks * 32u);
-                    const uint64_t bl = umma::sw128_desc(base + L.bl + ks * 32u);
-                    umma::mma_bf16(tm, ah, bl, idesc, ks > 0 ? 1u : 0u);
-                    umma::mma_bf16(tm, al, bh, idesc, 1u);
+                    for (uint32_t ks = 0; ks < (uint32_t)D / 16u; ++ks) {
+                        const uint64_t ah = umma::sw128_desc(sA + ks * 32u);
+                        const uint64_t al = umma::sw128_desc(sAl + ks * 32u);
+                        const uint64_t bh = umma::sw128_desc(base + L.bh + ks * 32u);
+                        const uint64_t bl = umma::sw128_desc(base + L.bl + ks * 32u);
+                        umma::mma_bf16(tm, ah, bl, idesc, ks > 0 ? 1u : 0u);
+                        umma::mma_bf16(tm, al, bh, idesc, 1u);
+                    }
+#pragma unroll
+                    for (uint32_t ks = 0; ks < (uint32_t)D / 16u; ++ks)
+                        umma::mma_bf16(tm, umma::sw128_desc(sA + ks * 32u),
+                                       umma::sw128_desc(base + L.bh + ks * 32u), idesc, 1u);
+                    umma::mma_commit(bar);
                 }
-#pragma unroll
-                for (uint32_t ks = 0; ks < (uint32_t)D / 16u; ++ks)
-                    umma::mma_bf16(tm, umma::sw128_desc(sA + ks * 32u), umma::sw128_desc(base + L.bh + ks * 32u), idesc,
-                                   1u);
-                umma::mma_commit(bar);
-                if (!umma_detail::wait_bounded(bar, phase)) *my_abort = 1u;
+                if (!umma_detail::wait_bounded(bar, phase, wait_ns)) *my_abort = 1u;
             }
             phase ^= 1u;
             umma_detail::half_sync(half);
@@ -517,7 +522,7 @@ __device__ __forceinline__ bool run_tiles_umma(const BatchJobDev& J, const float
         }
         // after an abort this half's last MMA may still be in flight: wait for it
         // (bounded) before the caller frees the accumulator
-        if (th == 0 && *my_abort) umma_detail::wait_bounded(bar, phase ^ 1u);
+        if (th == 0 && *my_abort) umma_detail::wait_bounded(bar, phase ^ 1u, wait_ns);
         __syncthreads();  // both halves are done with the chunk
         if (us.abort[0] || us.abort[1]) {
             if (threadIdx.x == 0) *s_abort = 1u;

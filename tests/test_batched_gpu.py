@@ -305,3 +305,39 @@ def test_batch_tensor_core_path_edge_values(ckm, oracle, cuda):
             assert np.array_equal(j["masses"].cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
     finally:
         b.close()
+
+
+def test_batch_tensor_core_wait_timeout_is_reported(ckm, oracle, cuda, monkeypatch):
+    """Failure detection without a GPU fault: with CKM_BATCH_TEST_STALL=1 the
+    first half of every CTA issues no MMA, so its bounded wait for the tensor
+    cores finds nothing and runs out (1 ms).  The CTA frees its tensor memory
+    and stops, the job is parked with the failed bit, ckm_batch_status
+    reports CKM_ERR_CUDA, and the context stays usable: a new batch afterwards
+    matches the oracle."""
+    import torch
+    monkeypatch.setenv("CKM_BATCH_TEST_STALL", "1")
+    jobs, _ = make_jobs(cuda, oracle, [(20000, 64, 64), (9000, 32, 40), (3000, 8, 10)], seed=31)
+    b = ckm.Batch(jobs, tile_points=1024, ctas_per_sm=1)
+    try:
+        b.step()
+        torch.cuda.synchronize()
+        with pytest.raises(ckm.CkmError) as e:
+            b.status()
+        assert "tensor cores" in str(e.value)
+    finally:
+        b.close()
+    monkeypatch.delenv("CKM_BATCH_TEST_STALL")
+    jobs, host = make_jobs(cuda, oracle, [(20000, 64, 64), (9000, 32, 40)], seed=32)
+    b = ckm.Batch(jobs, tile_points=1024, ctas_per_sm=1)
+    try:
+        Cin = [j["centroids"].cpu().numpy().copy() for j in jobs]
+        b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        for j, P, C0 in zip(jobs, host, Cin):
+            n, d, k = j["n"], j["d"], j["k"]
+            ref = oracle.label_f32(P, n, d, k, C0)
+            assert np.array_equal(j["labels"][:n].cpu().numpy().view(np.uint32), ref)
+        b.status()
+    finally:
+        b.close()
