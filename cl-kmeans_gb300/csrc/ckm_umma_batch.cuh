@@ -4,18 +4,19 @@
 // alternate 128-point sub-tiles (own point tiles, own 256 TMEM columns, own
 // mbarrier, own named barrier; the staged centroids are shared), so that one
 // half's MMA wait and merge overlap the other half's work.  Per sub-tile a
-// half splits every coordinate into two
-// fp16 halves, x = x_h + x_l (+ a residual of at most 2^-22 |x_f| + 2^-25),
-// writes both as K-major 128-byte-swizzled tiles, and one of its threads issues
-// x_h.c_h + x_h.c_l + x_l.c_h (tcgen05.mma kind::f16, M = 128 points,
-// N = k_pad clusters, K = 16 per instruction, f32 accumulation) into one
-// accumulator in tensor memory.  The centroids' halves are staged the same way
-// once per segment.  Each warp then reads the scores of its 32 points (its
-// TMEM lane quarter) for its half of the clusters, s_c = |c|^2 - 2 dot, keeps the
-// lowest two, and the certificate below decides the label.  Points it does not
-// prove take an exact candidate pass over the same scores (the reference's
-// arithmetic on the candidates), or the full exact scan when their values are
-// not finite.  The point sums use the FP32 coordinates held in registers.
+// half splits every coordinate into two fp16 halves, x = x_h + x_l (+ a
+// residual of at most 2^-22 |x_f| + 2^-25), writes both as K-major
+// 128-byte-swizzled tiles, and one of its threads issues x_h.c_l and x_l.c_h,
+// then x_h.c_h (tcgen05.mma kind::f16, M = 128 points, N = k_pad clusters,
+// K = 16 per instruction) into one f32 accumulator in tensor memory.  The
+// centroids' halves are staged the same way once per segment.  Each warp then
+// reads the scores of its 32 points (its TMEM lane quarter) for its half of
+// the clusters, s_c = |c|^2 - 2 dot, keeps the lowest two, and the
+// certificate below decides the label.  Points it does not prove are
+// deferred: their candidates (the clusters within T of the lowest score) are
+// resolved later with the reference's arithmetic; points whose values are not
+// finite take the full exact scan at once.  The point sums use the FP32
+// coordinates held in registers.
 //
 // Certificate.  With a >= |x|, cm >= max_c |c|, r = a + cm, eps = 2^-25 sqrt(D)
 // and gamma = 2 D 2^-23 (f32 accumulation, two ulps per addition of the
@@ -266,8 +267,10 @@ __device__ __forceinline__ void umma_resolve(const BatchJobDev& J, const float* 
 // Labels the points of tiles [t0, t1) of one job on the tensor cores and adds
 // them into the shared table (512 threads; two halves on alternate
 // sub-tiles).  bars: the halves' mbarriers (8 bytes apart); phase: this
-// thread's half's next phase.  Returns false when a wait for the tensor cores
-// ran out (every thread gets the same answer); the caller then stops.
+// thread's half's next phase.  test_stall: the failure-detection test (the
+// first half issues no MMA and its 1 ms wait runs out).  Returns false when a
+// wait for the tensor cores ran out (every thread gets the same answer); the
+// caller then stops.
 template <int D>
 __device__ __forceinline__ bool run_tiles_umma(const BatchJobDev& J, const float* __restrict__ C, uint32_t t0,
                                                uint32_t t1, uint32_t tile, uint32_t base, const UmmaLayout& L,
