@@ -565,9 +565,15 @@ int ckm_server_create(const ckm_server_options* options, ckm_server** out) {
     if ((e = cudaMemPoolCreate(&S->pool, &props)) != cudaSuccess) return cuda_fail(e, "server: cudaMemPoolCreate");
     uint64_t keep = ~0ull;  // memory returned to the pool stays there for the next jobs
     cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    // the batched lane's kernels run at the highest stream priority: when a
+    // large job's kernel ends, the next round's launch takes the SMs before
+    // the large job's next kernel, so small jobs do not queue behind it
+    int prio_low = 0, prio_high = 0;
+    if ((e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high)) != cudaSuccess)
+        return cuda_fail(e, "server: stream priorities");
     if ((e = cudaStreamCreateWithFlags(&S->s_up, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&S->s_comp, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&S->s_large, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithPriority(&S->s_comp, cudaStreamNonBlocking, prio_high)) != cudaSuccess ||
+        (e = cudaStreamCreateWithPriority(&S->s_large, cudaStreamNonBlocking, prio_low)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S->s_down, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&S->ev_up, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&S->ev_status, cudaEventDisableTiming)) != cudaSuccess ||
