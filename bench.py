@@ -574,7 +574,9 @@ def run_serving_workload(args, ckm, torch, dev):
 
     cap_rate = nb / burst_s
     spec = stream(args.serve_rate, args.serve_large_rate, args.serve_seconds, 7)
-    sustain = stream(0.7 * cap_rate, args.serve_large_rate, args.serve_seconds, 8)
+    # moderate load: 70 % of the configured small-job rate, same large jobs
+    # (the burst capacity ignores the device time the large jobs take)
+    sustain = stream(0.7 * args.serve_rate, args.serve_large_rate, args.serve_seconds, 8)
     line = {
         "metric": "jobs/s", "value": spec["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": spec["offered_jobs"],
         "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -584,7 +586,7 @@ def run_serving_workload(args, ckm, torch, dev):
                    "large_rate_per_s": args.serve_large_rate, "small_pool": len(pool), "tolerance": tol,
                    "max_iterations": cap, "round_iterations": args.serve_round or 4},
         "stream_at_config_rate": spec,
-        "stream_at_70pct_capacity": sustain,
+        "stream_at_70pct_config_rate": sustain,
         "burst_capacity_small_jobs_per_s": cap_rate,
         "burst_lane_stats": dict(burst_stats, wall_ns=int(burst_s * 1e9)),
         "plain_per_job_loop": {"jobs_per_s": 1.0 / plain_s, "jobs": nplain,
