@@ -158,6 +158,23 @@ def host_sample(n_s, d, blobs, slo, shi):
     return np.ascontiguousarray(X.astype(np.float32).T).reshape(-1)
 
 
+def ranks_max_ms(total_ms, world):
+    """The job's time over N replicas: the slowest rank's (an all-reduce MAX
+    over the process group; world 1: the rank's own)."""
+    if world <= 1:
+        return total_ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(total_ms)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, max_ms):
+    """Whole-job throughput: every rank's units over the slowest rank's time."""
+    return units_per_rank * world / (max_ms / 1e3)
+
+
 def run_reference_arm(args, workload):
     n, d, k, blobs, slo, shi, iters_cfg = WORKLOADS[workload]
     rank = env_int("RANK", 0)
@@ -788,10 +805,7 @@ def main():
         launches = ckm.launch_count() - launches0
         total_ms = t_start.elapsed_time(t_end)
         per_launch_ms = [a_.elapsed_time(b_) for a_, b_ in evs]
-        if world > 1:
-            t = torch.tensor([total_ms], dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms = ranks_max_ms(total_ms, world)
         return total_ms, per_launch_ms, launches
 
     for i in range(args.warmup):
@@ -826,9 +840,9 @@ def main():
     else:
         total_ms, per_launch_ms, gpu_launches = u_total_ms, u_per_launch, u_launches
     clocks = sampler.stop()
-    value = n * args.steps * world / (total_ms / 1e3)
+    value = replica_throughput(n * args.steps, world, total_ms)
     avg_launch_s = statistics.mean(per_launch_ms) / 1e3
-    unsorted = {"value": n * args.steps * world / (u_total_ms / 1e3), "ms_per_step": u_total_ms / args.steps,
+    unsorted = {"value": replica_throughput(n * args.steps, world, u_total_ms), "ms_per_step": u_total_ms / args.steps,
                 "call": "ckm_fused_f32 on the points in generation order"}
 
     # --- roofline of the fused kernel --------------------------------------
