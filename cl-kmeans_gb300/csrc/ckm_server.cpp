@@ -54,6 +54,7 @@ struct SJob {
     double* d_sums = nullptr;
     unsigned long long* d_msum = nullptr;
     int slot = -1;
+    uint64_t joined = 0;   // the first batched round the job is part of
 };
 
 // Byte layout of a small job's block.
@@ -101,13 +102,13 @@ struct ckm_server {
     // device
     cudaMemPool_t pool = nullptr;
     cudaStream_t s_up = nullptr, s_comp = nullptr, s_large = nullptr, s_down = nullptr;
-    cudaEvent_t ev_up = nullptr, ev_status = nullptr;
+    cudaEvent_t ev_up = nullptr, ev_status[2] = {nullptr, nullptr};
     BatchStatus* d_status = nullptr;   // [SLOTS]
     unsigned int* d_tickets = nullptr; // [SLOTS]
-    BatchStatus* h_status = nullptr;   // pinned copy
+    BatchStatus* h_status[2] = {nullptr, nullptr};  // pinned copies, one per round in flight
     std::vector<int> free_slots;
-    ::ckm_batch* batch = nullptr;
-    cudaEvent_t ev_s0 = nullptr, ev_s1 = nullptr;
+    ::ckm_batch* batch[2] = {nullptr, nullptr};  // job tables of the two rounds in flight
+    cudaEvent_t ev_s0[2] = {nullptr, nullptr}, ev_s1[2] = {nullptr, nullptr};
     ckm_server_stats stats{};  // written by the batched lane under mu
     // finished jobs of the batched lane, handed to the retire thread: their
     // results are copied out after the round's event, then they are released
@@ -283,20 +284,42 @@ uint64_t retiring_count(ckm_server* S) {
 }
 
 // The batched lane.  A round: the admitted jobs become the batch's table,
-// `round_iterations` launches advance them, the status comes back.  The host
-// work around a round overlaps the GPU: the next jobs' uploads are issued
-// while the round runs, and the finished jobs go to the retire thread, which
-// copies their results out on its own stream while the next round runs.
+// `round_iterations` launches advance them, the status comes back.  The lane
+// runs one round ahead: it launches round R, then reads the status of round
+// R - 1 while R runs, so the device never waits for the host between rounds.
+// Round R's table is built before R - 1's results are known, so it still
+// lists the jobs that stopped in R - 1; they are parked on the device (status
+// flags) and the kernel skips them, and their memory and status slots are
+// released only after R is done (the retire thread waits for an event
+// recorded behind R's launches).  The two rounds in flight use two batch
+// objects, two pinned status copies and two sets of events.  Uploads of the
+// next jobs are issued while the rounds run; finished jobs go to the retire
+// thread, which copies their results out on its own stream.
 void small_lane(ckm_server* S) {
     cudaSetDevice(S->device);
     const float tol = S->opt.tolerance;
     const uint32_t max_it = S->opt.max_iterations, rounds = S->opt.round_iterations;
     std::vector<SJob*> active, pending;
     std::vector<BatchJobDev> dev;
+    uint64_t round_id = 0;  // rounds launched so far
+    // the round launched last, whose status has not been read yet
+    bool in_flight = false;
+    int fl_par = 0;
+    uint64_t fl_id = 0;
+    int par = 0;
+    auto fail_all = [&](int st) {
+        cudaStreamSynchronize(S->s_comp);
+        for (SJob* j : active) {
+            release_small(S, j, S->s_comp);
+            finish(S, j, st, 0, 0, 0.f, 0);
+        }
+        active.clear();
+        in_flight = false;
+    };
     for (;;) {
         uint64_t admit_ns = 0, admitted = 0;
         take_and_admit(S, pending, admit_ns, admitted);
-        if (active.empty() && pending.empty()) {
+        if (active.empty() && pending.empty() && !in_flight) {
             std::unique_lock<std::mutex> lk(S->mu);
             if (S->stop && S->small_q.empty() && retiring_count(S) == 0) break;
             if (S->small_q.empty())
@@ -305,103 +328,122 @@ void small_lane(ckm_server* S) {
                 S->cv_work.wait_for(lk, std::chrono::milliseconds(1));
             continue;
         }
+        const auto t_round = Clock::now();
         if (!pending.empty()) {
             cudaEventRecord(S->ev_up, S->s_up);
             cudaStreamWaitEvent(S->s_comp, S->ev_up, 0);
+            for (SJob* j : pending) j->joined = round_id + 1;
             active.insert(active.end(), pending.begin(), pending.end());
             pending.clear();
         }
-        const auto t_round = Clock::now();
 
-        // one round over every admitted job
-        dev.resize(active.size());
-        int max_slot = 0;
-        for (size_t i = 0; i < active.size(); ++i) {
-            const SJob* j = active[i];
-            BatchJobDev& J = dev[i];
-            J.points = j->d_points;
-            J.cent[0] = j->d_cent[0];
-            J.cent[1] = j->d_cent[1];
-            J.labels = j->d_labels;
-            J.masses = j->d_masses;
-            J.sums = j->d_sums;
-            J.msum = j->d_msum;
-            J.ticket = S->d_tickets + j->slot;
-            J.status = S->d_status + j->slot;
-            J.n = j->u.num_points;
-            J.d = j->u.num_features;
-            J.k = j->u.num_clusters;
-            J.num_tiles = 0;
-            J.pad = 0;
-            max_slot = std::max(max_slot, j->slot);
-        }
-        // one 512-thread CTA per SM with the whole shared memory (room for the
-        // tensor-core centroid fragments of d = 32 / 64 jobs), 4096-point tiles
-        int st = batch_set_jobs(S->batch, dev.data(), (uint32_t)dev.size(), 4096, 1, tol, max_it, S->s_comp);
-        cudaEventRecord(S->ev_s0, S->s_comp);
-        for (uint32_t r = 0; r < rounds && st == CKM_OK; ++r) st = batch_launch_step(S->batch, S->s_comp);
-        cudaEventRecord(S->ev_s1, S->s_comp);
-        cudaError_t e = cudaSuccess;
-        if (st == CKM_OK) {
-            e = cudaMemcpyAsync(S->h_status, S->d_status, (size_t)(max_slot + 1) * sizeof(BatchStatus),
-                                cudaMemcpyDeviceToHost, S->s_comp);
-            if (e == cudaSuccess) e = cudaEventRecord(S->ev_status, S->s_comp);
-            // while the round runs: the next jobs' uploads
-            take_and_admit(S, pending, admit_ns, admitted);
-            if (e == cudaSuccess) e = cudaEventSynchronize(S->ev_status);
-            if (e != cudaSuccess) st = cuda_fail(e, "server: status read-back");
+        // launch round round_id + 1 over every admitted job
+        bool launched = false;
+        int st = CKM_OK;
+        if (!active.empty()) {
+            dev.resize(active.size());
+            int max_slot = 0;
+            for (size_t i = 0; i < active.size(); ++i) {
+                const SJob* j = active[i];
+                BatchJobDev& J = dev[i];
+                J.points = j->d_points;
+                J.cent[0] = j->d_cent[0];
+                J.cent[1] = j->d_cent[1];
+                J.labels = j->d_labels;
+                J.masses = j->d_masses;
+                J.sums = j->d_sums;
+                J.msum = j->d_msum;
+                J.ticket = S->d_tickets + j->slot;
+                J.status = S->d_status + j->slot;
+                J.n = j->u.num_points;
+                J.d = j->u.num_features;
+                J.k = j->u.num_clusters;
+                J.num_tiles = 0;
+                J.pad = 0;
+                max_slot = std::max(max_slot, j->slot);
+            }
+            // one 512-thread CTA per SM with the whole shared memory (room for
+            // the tensor-core tiles of d = 32 / 64 jobs), 4096-point tiles
+            st = batch_set_jobs(S->batch[par], dev.data(), (uint32_t)dev.size(), 4096, 1, tol, max_it, S->s_comp);
+            cudaEventRecord(S->ev_s0[par], S->s_comp);
+            for (uint32_t r = 0; r < rounds && st == CKM_OK; ++r) st = batch_launch_step(S->batch[par], S->s_comp);
+            cudaEventRecord(S->ev_s1[par], S->s_comp);
+            if (st == CKM_OK) {
+                cudaError_t e = cudaMemcpyAsync(S->h_status[par], S->d_status,
+                                                (size_t)(max_slot + 1) * sizeof(BatchStatus), cudaMemcpyDeviceToHost,
+                                                S->s_comp);
+                if (e == cudaSuccess) e = cudaEventRecord(S->ev_status[par], S->s_comp);
+                if (e != cudaSuccess) st = cuda_fail(e, "server: status read-back");
+            }
+            launched = st == CKM_OK;
         }
         if (st != CKM_OK) {  // the round failed: its jobs fail with the reason
-            cudaStreamSynchronize(S->s_comp);
-            for (SJob* j : active) {
-                release_small(S, j, S->s_comp);
-                finish(S, j, st, 0, 0, 0.f, 0);
-            }
-            active.clear();
+            fail_all(st);
             continue;
         }
+        if (launched) ++round_id;
+
+        // while it runs: the next jobs' uploads, and the round before it
+        take_and_admit(S, pending, admit_ns, admitted);
+        const size_t njobs = active.size();
+        size_t ndone = 0;
         float steps_ms = 0.f;
-        cudaEventElapsedTime(&steps_ms, S->ev_s0, S->ev_s1);
         const auto t_retire = Clock::now();
-        // the jobs that stopped in this round go to the retire thread
-        std::vector<SJob*> keep;
-        ckm_server::Retiring r;
-        for (SJob* j : active) {
-            const BatchStatus& b = S->h_status[j->slot];
-            if (!(b.flags & 2u)) {
-                keep.push_back(j);
+        if (in_flight) {
+            const cudaError_t e = cudaEventSynchronize(S->ev_status[fl_par]);
+            if (e != cudaSuccess) {
+                fail_all(cuda_fail(e, "server: status read-back"));
                 continue;
             }
-            r.jobs.push_back(j);
-            r.status.push_back(b);
-        }
-        if (!r.jobs.empty()) {
-            cudaEvent_t ev = nullptr;
-            {
-                std::lock_guard<std::mutex> g(S->rmu);
-                if (!S->free_events.empty()) {
-                    ev = S->free_events.back();
-                    S->free_events.pop_back();
+            cudaEventElapsedTime(&steps_ms, S->ev_s0[fl_par], S->ev_s1[fl_par]);
+            // the jobs of that round that stopped go to the retire thread; the
+            // event is recorded behind the round launched above, which still
+            // lists them
+            std::vector<SJob*> keep;
+            ckm_server::Retiring r;
+            for (SJob* j : active) {
+                const BatchStatus& b = S->h_status[fl_par][j->slot];
+                if (j->joined > fl_id || !(b.flags & 2u)) {
+                    keep.push_back(j);
+                    continue;
                 }
+                r.jobs.push_back(j);
+                r.status.push_back(b);
             }
-            if (!ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-            r.ev = ev;
-            // the results are final once the round's kernels are done
-            cudaEventRecord(r.ev, S->s_comp);
-            {
-                std::lock_guard<std::mutex> g(S->rmu);
-                S->retiring_jobs += r.jobs.size();
-                S->retire_q.push_back(std::move(r));
+            if (!r.jobs.empty()) {
+                cudaEvent_t ev = nullptr;
+                {
+                    std::lock_guard<std::mutex> g(S->rmu);
+                    if (!S->free_events.empty()) {
+                        ev = S->free_events.back();
+                        S->free_events.pop_back();
+                    }
+                }
+                if (!ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+                r.ev = ev;
+                cudaEventRecord(r.ev, S->s_comp);
+                {
+                    std::lock_guard<std::mutex> g(S->rmu);
+                    S->retiring_jobs += r.jobs.size();
+                    S->retire_q.push_back(std::move(r));
+                }
+                S->cv_retire.notify_one();
             }
-            S->cv_retire.notify_one();
+            ndone = active.size() - keep.size();
+            active.swap(keep);
         }
-        const size_t ndone = active.size() - keep.size();
+        in_flight = launched;
+        if (launched) {
+            fl_par = par;
+            fl_id = round_id;
+            par ^= 1;
+        }
         const auto t_end = Clock::now();
         {
             std::lock_guard<std::mutex> g(S->mu);
             ckm_server_stats& x = S->stats;
-            x.rounds += 1;
-            x.job_rounds += active.size();
+            x.rounds += launched ? 1 : 0;
+            x.job_rounds += launched ? njobs : 0;
             x.busy_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t_end - t_round).count();
             x.steps_gpu_ns += (uint64_t)(steps_ms * 1e6);
             x.admit_ns += admit_ns;
@@ -409,7 +451,6 @@ void small_lane(ckm_server* S) {
             x.jobs_admitted += admitted;
             x.jobs_completed += ndone;
         }
-        active.swap(keep);
     }
 }
 
@@ -576,16 +617,20 @@ int ckm_server_create(const ckm_server_options* options, ckm_server** out) {
         (e = cudaStreamCreateWithPriority(&S->s_large, cudaStreamNonBlocking, prio_low)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S->s_down, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&S->ev_up, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&S->ev_status, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaEventCreate(&S->ev_s0)) != cudaSuccess || (e = cudaEventCreate(&S->ev_s1)) != cudaSuccess)
+        (e = cudaEventCreateWithFlags(&S->ev_status[0], cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&S->ev_status[1], cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreate(&S->ev_s0[0])) != cudaSuccess || (e = cudaEventCreate(&S->ev_s1[0])) != cudaSuccess ||
+        (e = cudaEventCreate(&S->ev_s0[1])) != cudaSuccess || (e = cudaEventCreate(&S->ev_s1[1])) != cudaSuccess)
         return cuda_fail(e, "server: streams");
     if ((e = cudaMalloc(&S->d_status, SLOTS * sizeof(BatchStatus))) != cudaSuccess ||
         (e = cudaMalloc(&S->d_tickets, SLOTS * sizeof(unsigned int))) != cudaSuccess ||
-        (e = cudaMallocHost(&S->h_status, SLOTS * sizeof(BatchStatus))) != cudaSuccess)
+        (e = cudaMallocHost(&S->h_status[0], SLOTS * sizeof(BatchStatus))) != cudaSuccess ||
+        (e = cudaMallocHost(&S->h_status[1], SLOTS * sizeof(BatchStatus))) != cudaSuccess)
         return cuda_fail(e, "server: status slots");
     S->free_slots.resize(SLOTS);
     for (uint32_t i = 0; i < SLOTS; ++i) S->free_slots[i] = (int)(SLOTS - 1 - i);
-    int st = batch_create_external(&S->batch);
+    int st = batch_create_external(&S->batch[0]);
+    if (st == CKM_OK) st = batch_create_external(&S->batch[1]);
     if (st) return st;
     ckm_server* raw = S.release();
     raw->retire_thread = std::thread(retire_loop, raw);
@@ -669,14 +714,16 @@ int ckm_server_destroy(ckm_server* S) {
     for (cudaEvent_t ev : S->free_events) cudaEventDestroy(ev);
     cudaSetDevice(S->device);
     cudaDeviceSynchronize();
-    ckm_batch_destroy(S->batch);
+    for (int i = 0; i < 2; ++i) {
+        ckm_batch_destroy(S->batch[i]);
+        cudaFreeHost(S->h_status[i]);
+        cudaEventDestroy(S->ev_status[i]);
+        cudaEventDestroy(S->ev_s0[i]);
+        cudaEventDestroy(S->ev_s1[i]);
+    }
     cudaFree(S->d_status);
     cudaFree(S->d_tickets);
-    cudaFreeHost(S->h_status);
     cudaEventDestroy(S->ev_up);
-    cudaEventDestroy(S->ev_status);
-    cudaEventDestroy(S->ev_s0);
-    cudaEventDestroy(S->ev_s1);
     cudaStreamDestroy(S->s_up);
     cudaStreamDestroy(S->s_comp);
     cudaStreamDestroy(S->s_large);
