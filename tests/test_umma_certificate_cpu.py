@@ -150,3 +150,27 @@ def test_certified_labels_are_the_reference_labels(D, spread):
         assert not np.any(proved[ref == 0])
         assert np.any(ref == 0)
         assert proved.mean() > 0.2
+
+
+def _header_constants(D):
+    """UmmaBound<D>'s constants, evaluated from the header's own expressions."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(__file__), "..", "cl-kmeans_gb300", "csrc", "ckm_umma_batch.cuh")).read()
+    body = re.search(r"struct UmmaBound \{(.*?)\n\};", src, re.S).group(1)
+    env = {"D": D}
+    for name in ("gamma", "A", "B", "C"):
+        expr = re.search(r"static constexpr float %s\s*=\s*(.*?);" % name, body, re.S).group(1)
+        expr = re.sub(r"0x1p(-?\d+)f", r"(2.0 ** \1)", expr)
+        expr = re.sub(r"(\d+\.\d+)f", r"\1", expr).replace("(float)", "")
+        expr = re.sub(r"\(D == 64 \? ([\d.]+) : ([\d.]+)\)", r"(\1 if D == 64 else \2)", expr)
+        env[name] = eval(expr, {}, env)
+    return env["A"], env["B"], env["C"]
+
+
+@pytest.mark.parametrize("D", [32, 64])
+def test_emulated_bound_is_the_kernels(D):
+    """The constants checked above are the ones the kernel uses."""
+    got = _header_constants(D)
+    for a, b in zip(got, bound_constants(D)):
+        assert a == pytest.approx(b, rel=1e-6)
