@@ -12,6 +12,9 @@ proved has the reference's label.
     the tensor core (low 13 bits dropped); three chains (c_mid x_hi,
     c_hi x_mid, c_hi x_hi) added at the end; T = ((D + 8) 2^-22 +
     (2D + 8) 2^-24) r^2 (1.001), the score part being (D + 8) 2^-23 r^2.
+  * Config 3's tensor-core label kernel (ckm_tc.cu): points and centroids
+    scaled by powers of two and rounded once to fp16, one f32 chain, a T
+    built from the measured rounding-error norms of both operands.
 """
 import numpy as np
 import pytest
@@ -116,5 +119,64 @@ def test_tf32_screen_score_error_within_its_share_of_T(D, scale):
     r, cn = r_bound(X, C)
     s = tf32_screen_scores(X, C, cn).astype(np.float64)
     share = (D + 8) * 2.0 ** -23 * r * r * 1.001
+    err = np.abs(s - exact_scores(X, C)).max(1)
+    assert np.all(err <= share), float((err / share).max())
+
+
+def _scale_exponent(maxabs):
+    """2^e * maxabs <= 2^15 (fp16 safe), e in [-60, 60] (ckm_tc.cu)."""
+    if not maxabs > 0 or not np.isfinite(maxabs):
+        return 0
+    _, e = np.frexp(np.float32(maxabs))
+    return int(min(60, max(-60, 15 - int(e))))
+
+
+def tc_scores_and_threshold(X, C, d_pad):
+    """The config-3 tensor-core label kernel's scores and its T per point
+    (tc_points_convert_kernel, tc_centroid_stats/pack_kernel, tc_params_kernel),
+    with the f32 accumulation of the MMA done sequentially in K = 16 blocks."""
+    n, d = X.shape
+    sx = 2.0 ** _scale_exponent(float(np.abs(X).max()))
+    sc = 2.0 ** _scale_exponent(float(np.abs(C).max()))
+    xs = f32(X.astype(np.float64) * sx)
+    cs = f32(C.astype(np.float64) * sc)
+    xh = xs.astype(np.float16).astype(np.float32)
+    ch = cs.astype(np.float16).astype(np.float32)
+    xn = np.sqrt((X.astype(np.float64) ** 2).sum(1) * (1 + 2.0 ** -14)) * (1 + 2.0 ** -20)
+    xe = (np.sqrt(((xh.astype(np.float64) - xs) ** 2).sum(1) * (1 + 2.0 ** -14)) * (1 + 2.0 ** -20)
+          + d * 2.0 ** -149) / sx
+    csum = (C.astype(np.float64) ** 2).sum(1)
+    cn = f32(csum)
+    cm = np.sqrt(csum).max() * (1 + 2.0 ** -40)
+    fm = ((np.sqrt(((ch.astype(np.float64) - cs) ** 2).sum(1)) * (1 + 2.0 ** -40) + d * 2.0 ** -149) / sc).max()
+    acc = np.zeros((n, C.shape[0]), np.float32)
+    for f in range(d):  # zero padding up to d_pad adds nothing
+        acc = f32(acc.astype(np.float64) + f32(xh[:, None, f].astype(np.float64) * ch[None, :, f]))
+    alpha = -2.0 / (sx * sc)
+    s = fma32(alpha, acc, cn[None, :])
+    gam, safety = 2.0 * d_pad * 2.0 ** -23, 1.0 + 2.0 ** -10
+    t1 = (4.0 * fm + 4.0 * gam * (cm + fm)) * safety
+    te = (4.0 * (cm + fm) + 4.0 * gam * (cm + fm)) * safety
+    rho2 = 2.0 * (d + 2.0) * 2.0 ** -24 * 1.01 * safety
+    t2 = 2.0 * 2.0 ** -23 * 1.01 * safety + rho2
+    t0 = (d + 8.0) * 2.0 ** -146
+    r = xn + cm
+    T = (t2 * r * r + te * xe + t1 * xn + t0) * (1 + 2.0 ** -10)
+    share = (T - rho2 * r * r) / 2.0
+    return s.astype(np.float64), share
+
+
+@pytest.mark.parametrize("d", [64, 128])
+@pytest.mark.parametrize("scale", [1e-3, 2.0, 500.0])
+def test_tensor_core_certificate_bounds_its_score_error(d, scale):
+    """Config 3's fp16 certificate (single chain, measured rounding errors of
+    the operands): the score error stays within half of T minus the
+    reference's own distance error."""
+    rng = np.random.default_rng(d + int(scale * 10))
+    X = (rng.normal(0, 1, (120, d)) * scale).astype(np.float32)
+    C = (rng.normal(0, 1, (32, d)) * scale).astype(np.float32)
+    X[:4] = C[:4]
+    X[4:8] *= np.float32(2.0 ** -12)  # small points next to large centroids
+    s, share = tc_scores_and_threshold(X, C, d_pad=(d + 63) // 64 * 64)
     err = np.abs(s - exact_scores(X, C)).max(1)
     assert np.all(err <= share), float((err / share).max())
