@@ -369,9 +369,12 @@ typedef struct ckm_run_config {
     int converge;                          /* kmeans.converge: stop once the relative centroid shift
                                               (ckm_centroid_shift_*) falls below tolerance */
     double tolerance;                      /* 0 = 1e-4 */
-    int spatial_order;                     /* single_stage, FP32, d <= 8, k <= 32: run the iterations on
-                                              a spatially ordered copy (ckm_spatial_sort_f32, box-pruned
-                                              ckm_fused_sorted_f32; labels mapped back at the end).
+    int spatial_order;                     /* single_stage and three_stage, FP32, d <= 8, k <= 32: run
+                                              the iterations on a spatially ordered copy
+                                              (ckm_spatial_sort_f32, then the box-pruned
+                                              ckm_fused_sorted_f32 / ckm_labeling_sorted_f32); the
+                                              last iteration labels the caller's order directly (an
+                                              unpermute only when the run stops early).
                                               0 = auto (n >= 2^20, >= 8 iterations, device memory
                                               allows), 1 = whenever the shape allows, -1 = never */
 } ckm_run_config;
