@@ -387,7 +387,7 @@ int ckm_batch_status(ckm_batch* b, float* shifts, uint32_t* iterations, ckm_stre
         if ((st[j].flags & 4u) && failed == 0xffffffffu) failed = j;
     }
     if (failed != 0xffffffffu)
-        return fail(CKM_ERR_CUDA, "batched: a wait for the tensor cores timed out (job " + std::to_string(failed) +
+        return fail(CKM_ERR_TIMEOUT, "batched: a wait for the tensor cores timed out (job " + std::to_string(failed) +
                                       " failed and is skipped by later steps)");
     return CKM_OK;
 }

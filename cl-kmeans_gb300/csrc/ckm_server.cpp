@@ -266,7 +266,7 @@ void retire_loop(ckm_server* S) {
             release_small(S, j, S->s_down);
             int st = e == cudaSuccess ? CKM_OK : cuda_fail(e, "server: results");
             if (st == CKM_OK && (b.flags & 4u))
-                st = fail(CKM_ERR_CUDA, "server: a wait for the tensor cores timed out in the job's round");
+                st = fail(CKM_ERR_TIMEOUT, "server: a wait for the tensor cores timed out in the job's round");
             finish(S, j, st, b.iterations, (tol > 0.f && b.shift < tol) ? 1u : 0u, b.shift, 0);
         }
         {

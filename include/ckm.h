@@ -300,7 +300,9 @@ typedef struct ckm_batch_job {
 
 typedef struct ckm_batch_options {
     uint32_t tile_points;   /* points per tile; 0 = choose (autotune or default) */
-    uint32_t ctas_per_sm;   /* 0 = choose; 1 = one 512-thread CTA per SM, 2 or more = 256-thread CTAs */
+    uint32_t ctas_per_sm;   /* 0 = choose; 1 = one 512-thread CTA per SM (d = 32 / 64 jobs with
+                               16 <= k <= 256 then label on the tcgen05 tensor cores), 2 or more =
+                               256-thread CTAs (TF32 mma.sync screen for d = 32 / 64) */
     uint32_t flush_tiles;   /* tiles between FP64 merges of a CTA's partial sums; 0 = 16 */
     int autotune;           /* time candidate tile sizes / CTA counts on the batch itself */
     float tolerance;        /* > 0: a job stops (is skipped by later steps) once its relative centroid

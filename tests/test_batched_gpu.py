@@ -324,6 +324,7 @@ def test_batch_tensor_core_wait_timeout_is_reported(ckm, oracle, cuda, monkeypat
         with pytest.raises(ckm.CkmError) as e:
             b.status()
         assert "tensor cores" in str(e.value)
+        assert e.value.status == -7  # CKM_ERR_TIMEOUT
     finally:
         b.close()
     monkeypatch.delenv("CKM_BATCH_TEST_STALL")
