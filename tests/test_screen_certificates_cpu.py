@@ -180,3 +180,51 @@ def test_tensor_core_certificate_bounds_its_score_error(d, scale):
     s, share = tc_scores_and_threshold(X, C, d_pad=(d + 63) // 64 * 64)
     err = np.abs(s - exact_scores(X, C)).max(1)
     assert np.all(err <= share), float((err / share).max())
+
+
+def _reference_labels(X, C):
+    """The reference's FP32 distances and strict '<' argmin from cluster 0."""
+    n, D = X.shape
+    acc = np.zeros((n, C.shape[0]), np.float32)
+    for f in range(D):
+        t = f32(X[:, None, f].astype(np.float64) - C[None, :, f])
+        acc = fma32(t, t, acc)
+    best = np.full(n, np.finfo(np.float32).max, np.float32)
+    lab = np.zeros(n, np.int64)
+    for c in range(C.shape[0]):
+        lt = acc[:, c] < best
+        best = np.where(lt, acc[:, c], best)
+        lab = np.where(lt, c, lab)
+    return lab
+
+
+def _near_ties(rng, D, n=600, k=16, spread=1e-3):
+    centres = rng.uniform(-10, 10, (k - k // 4, D))
+    C = np.concatenate([centres, centres[: k // 4] + rng.normal(0, spread, (k // 4, D))]).astype(np.float32)
+    C[1] = C[0]
+    X = (C[rng.integers(0, k, n)] + rng.normal(0, 1.0, (n, D))).astype(np.float32)
+    return X, C
+
+
+@pytest.mark.parametrize("D,screen", [(8, "fp32"), (32, "fp32"), (64, "fp32"), (32, "tf32"), (64, "tf32")])
+def test_certified_labels_are_the_reference_labels(D, screen):
+    """Near ties (duplicated and almost duplicated centroids): a label the
+    screen certifies (m2 - m1 > T) is the reference's; the others go to the
+    exact pass in the kernels."""
+    rng = np.random.default_rng(D * 3 + len(screen))
+    X, C = _near_ties(rng, D)
+    ref = _reference_labels(X, C)
+    r, cn = r_bound(X, C)
+    if screen == "fp32":
+        s = fp32_screen_scores(X, C, cn)
+        T = ((4 * D + 32) * U * r * r + 2.0 ** -126) * 1.001
+    else:
+        s = tf32_screen_scores(X, C, cn)
+        T = ((D + 8) * 2.0 ** -22 + (2 * D + 8) * 2.0 ** -24) * 1.001 * r * r + 2.0 ** -117 * (r + 1)
+    order = np.argsort(s, axis=1, kind="stable")
+    m1 = s[np.arange(len(X)), order[:, 0]].astype(np.float64)
+    m2 = s[np.arange(len(X)), order[:, 1]].astype(np.float64)
+    proved = (m2 - m1) > T
+    assert np.all(order[proved, 0] == ref[proved])
+    assert not np.any(proved[ref == 0])  # the duplicated pair 0 / 1 is never proved
+    assert proved.mean() > 0.3
