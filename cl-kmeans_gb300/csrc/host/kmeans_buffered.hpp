@@ -24,6 +24,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstring>
 #include <stdexcept>
 #include <thread>
 #include <vector>
