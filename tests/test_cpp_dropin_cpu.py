@@ -100,3 +100,22 @@ def test_reference_style_program_compiles_links_and_loads(ckm, tmp_path):
     assert r.returncode == 0, r.stdout[-4000:]
     r = subprocess.run([str(exe)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=60)
     assert r.returncode == 0, r.stdout[-2000:]
+
+
+def test_every_public_header_compiles_on_its_own():
+    """Each C++ header of the drop-in surface includes what it uses, and the
+    C ABI header is valid C (what cgo / other FFIs see)."""
+    import glob
+    cxx, cc = shutil.which("g++"), shutil.which("gcc")
+    if cxx is None or cc is None:
+        pytest.skip("no g++ / gcc")
+    cuda_inc = os.path.join(_cuda_home(), "include")
+    host = os.path.join(ROOT, "cl-kmeans_gb300", "csrc", "host")
+    inc = os.path.join(ROOT, "include")
+    for h in sorted(glob.glob(os.path.join(host, "*.hpp"))):
+        r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-x", "c++", "-I", host, "-I", inc, "-I", cuda_inc, h],
+                           stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
+        assert r.returncode == 0, (h, r.stdout[-2000:])
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-x", "c", os.path.join(inc, "ckm.h")],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout[-2000:]
