@@ -28,12 +28,17 @@ public:
         return create_engine(config, measurement);
     }
 
+    // The strategy names create() accepts; others throw (fused_factory.hpp:83-85).
+    static bool known(const std::string& strategy) {
+        return strategy == "cluster_merge" || strategy == "feature_sum";
+    }
+
     // The functor's object, for strategies that also run whole-iteration launches.
     FusedLloyd<PointT, LabelT, MassT> create_engine(FusedConfiguration config, Measurement::Measurement& measurement) {
         measurement.set_parameter("FusedGlobalSize", std::to_string(config.global_size[0]));
         measurement.set_parameter("FusedLocalSize", std::to_string(config.local_size[0]));
         measurement.set_parameter("FusedVectorLength", std::to_string(config.vector_length));
-        if (config.strategy == "cluster_merge" || config.strategy == "feature_sum") {
+        if (known(config.strategy)) {
             FusedLloyd<PointT, LabelT, MassT> strategy;
             strategy.prepare(config);
             return strategy;
@@ -52,10 +57,13 @@ public:
         BufferIterator<LabelT> labels_begin, BufferIterator<LabelT> labels_end, Measurement::DataPoint& datapoint,
         WaitList const& events)>;
 
+    // The strategy names create() accepts; others throw (labeling_factory.hpp:82-84).
+    static bool known(const std::string& strategy) { return strategy == "unroll_vector"; }
+
     LabelingFunction create(LabelingConfiguration config, Measurement::Measurement& measurement) {
         measurement.set_parameter("LabelingGlobalSize", std::to_string(config.global_size[0]));
         measurement.set_parameter("LabelingLocalSize", std::to_string(config.local_size[0]));
-        if (config.strategy == "unroll_vector") {
+        if (known(config.strategy)) {
             measurement.set_parameter("LabelingVectorLength", std::to_string(config.vector_length));
             measurement.set_parameter("LabelingUnrollClustersLength", std::to_string(config.unroll_clusters_length));
             measurement.set_parameter("LabelingUnrollFeaturesLength", std::to_string(config.unroll_features_length));
@@ -75,13 +83,18 @@ public:
         BufferIterator<LabelT> labels_end, BufferIterator<MassT> masses_begin, BufferIterator<MassT> masses_end,
         Measurement::DataPoint& datapoint, WaitList const& events)>;
 
+    // The strategy names create() accepts; others throw (mass_update_factory.hpp:91-93).
+    static bool known(const std::string& strategy) {
+        return strategy == "global_atomic" || strategy == "part_global" || strategy == "part_local" ||
+               strategy == "part_private";
+    }
+
     MassUpdateFunction create(MassUpdateConfiguration config, Measurement::Measurement& measurement) {
         measurement.set_parameter("MassUpdateGlobalSize", std::to_string(config.global_size[0]));
         measurement.set_parameter("MassUpdateLocalSize", std::to_string(config.local_size[0]));
         if (config.strategy == "part_private")
             measurement.set_parameter("MassUpdateVectorLength", std::to_string(config.vector_length));
-        if (config.strategy == "global_atomic" || config.strategy == "part_global" ||
-            config.strategy == "part_local" || config.strategy == "part_private") {
+        if (known(config.strategy)) {
             MassUpdate<LabelT, MassT> strategy;
             strategy.prepare(config);
             return strategy;
@@ -102,6 +115,11 @@ public:
 
     CentroidUpdateFunction create(CentroidUpdateConfiguration config, Measurement::Measurement& measurement) {
         return create_engine(config, measurement);
+    }
+
+    // The strategy names create() accepts; others throw (centroid_update_factory.hpp:121-123).
+    static bool known(const std::string& strategy) {
+        return strategy == "feature_sum" || strategy == "feature_sum_pardim" || strategy == "cluster_merge";
     }
 
     CentroidUpdate<PointT, LabelT, MassT> create_engine(CentroidUpdateConfiguration config,

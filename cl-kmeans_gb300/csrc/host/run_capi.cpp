@@ -41,6 +41,21 @@ int run_impl(const ckm_run_config* cfg, uint32_t iters, uint32_t d, uint64_t n, 
     if (n > 0 && (!points || !labels)) return ckm::fail(CKM_ERR_INVALID_ARGUMENT, "points/labels NULL");
     if (!centroids || !masses) return ckm::fail(CKM_ERR_INVALID_ARGUMENT, "centroids/masses NULL");
     const std::string pipeline = or_default(cfg->pipeline, "single_stage");
+    // names are checked before any device work, as the reference's factories
+    // reject an unknown strategy when they are configured
+    const bool single = pipeline == "single_stage" || pipeline == "single_stage_buffered";
+    const bool three = pipeline == "three_stage" || pipeline == "three_stage_buffered";
+    if (!single && !three) return ckm::fail(CKM_ERR_UNKNOWN_STRATEGY, "unknown pipeline '" + pipeline + "'");
+    const std::string fused = or_default(cfg->fused_strategy, "feature_sum");
+    const std::string labeling = or_default(cfg->labeling_strategy, "unroll_vector");
+    const std::string mass = or_default(cfg->mass_update_strategy, "part_local");
+    const std::string update = or_default(cfg->centroid_update_strategy, "feature_sum");
+    const char* bad = nullptr;
+    if (single && !FusedFactory<P, L, M, true>::known(fused)) bad = fused.c_str();
+    if (three && !LabelingFactory<P, L, true>::known(labeling)) bad = labeling.c_str();
+    if (three && !MassUpdateFactory<L, M>::known(mass)) bad = mass.c_str();
+    if (three && !CentroidUpdateFactory<P, L, M, true>::known(update)) bad = update.c_str();
+    if (bad) return ckm::fail(CKM_ERR_UNKNOWN_STRATEGY, std::string("unknown strategy: ") + bad);
     const uint64_t launches0 = ckm::launch_count();
     try {
         if (cfg->device >= 0) cuda_check(cudaSetDevice(cfg->device), "cudaSetDevice");
