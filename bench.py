@@ -90,10 +90,13 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    # where the raw samples go: $CKM_CLOCKS_CSV if set, else a temporary file
     def __init__(self, gpu_index):
+        import tempfile
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.path = os.environ.get("CKM_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(),
+                                                                     "ckm_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
