@@ -63,3 +63,25 @@ def test_single_rank_is_its_own_time():
     import bench
     assert bench.ranks_max_ms(42.0, 1) == 42.0
     assert bench.replica_throughput(500, 1, 250.0) == pytest.approx(2000.0)
+
+
+def test_reference_arm_line_on_the_cpu():
+    """bench.py --impl reference times the reference's CPU path (the oracle
+    port of KmeansNaive) on the host cores and prints one JSON line with the
+    contract's keys; it needs no GPU."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600,
+                       cwd=ROOT)
+    assert r.returncode == 0, r.stdout[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["metric"] == "pts*iter/s" and line["unit"] == "pts*iter/s" and line["value"] > 0
+    assert line["higher_is_better"] is True and line["warmup"] >= 3
+    cpu = line["cpu_baseline"]
+    assert cpu["kind"] in ("port", "reference") and cpu["cores"] >= 1 and cpu["sample"]
+    assert cpu["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["workload"] == "lloyd_n2^28_d4_k16"
