@@ -1,17 +1,21 @@
 // Serving loop: continuous batching of independent k-means jobs.
 //
-// Two worker threads per server:
+// Three worker threads per server:
 //   - the batched lane admits small jobs into device memory (a stream-ordered
 //     pool, within the byte budget), then runs rounds: the batch's job table
 //     is replaced by the admitted jobs, `round_iterations` persistent
 //     launches advance all of them (each parks itself on the device at its
-//     own stopping iteration: shift below the tolerance or the cap), one
-//     status read-back per round retires the finished ones (results copied
-//     back, memory returned to the pool).  Arrivals join at the next round.
-//   - the large-job lane runs jobs with n*k*d >= large_work one at a time:
-//     on the tensor cores (ckm_tc_fused_f32) when the device and shape allow
-//     and d >= 32, else with ckm_fused_f32; the convergence test after every
-//     iteration (ckm_centroid_shift_f32).
+//     own stopping iteration: shift below the tolerance or the cap), and one
+//     status read-back per round finds the finished ones.  The lane runs one
+//     round ahead (it reads round R - 1's status while R runs), on a stream of
+//     the highest priority.  Arrivals join at the next round.
+//   - the retire thread copies finished jobs' results to the caller's arrays
+//     on its own stream and returns their memory and status slots, after the
+//     last round that lists them is done.
+//   - the large-job lane runs jobs with n*k*d >= large_work one at a time, on
+//     a stream of the lowest priority: on the tensor cores (ckm_tc_fused_f32)
+//     when the device and shape allow and d >= 32, else with ckm_fused_f32;
+//     the convergence test after every iteration (ckm_centroid_shift_f32).
 // Job state per small job lives for the job's whole life: points, labels,
 // the centroid pair, masses, FP64 scratch, and a status/ticket slot in two
 // server-wide arrays, so a job keeps its iteration count and centroid parity
