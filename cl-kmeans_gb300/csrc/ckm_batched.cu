@@ -8,9 +8,12 @@
 // estimated cost left most SMs idle behind a few slow CTAs, because small-k
 // jobs pay for shared-memory atomic contention that the estimate does not
 // see).  Per segment a CTA stages the job's centroids in shared memory,
-// labels each point with the reference's exact arithmetic (fma(t,t,acc) over
-// the features, strict '<' argmin from cluster 0; kmeans_naive.cpp:48-63) and
-// adds it into a shared-memory sum/mass table, which it merges into the job's
+// labels each point with the reference's result (fma(t,t,acc) over the
+// features, strict '<' argmin from cluster 0; kmeans_naive.cpp:48-63): the
+// exact loop for d = 2 / 4, a certified FP32 screen in front of it for
+// d >= 8, and for d = 32 / 64 a certified tensor-core screen (the tcgen05 path
+// of ckm_umma_batch.cuh in 512-thread CTAs, else TF32 mma.sync), and adds each
+// point into a shared-memory sum/mass table, which it merges into the job's
 // FP64 scratch every `flush` tiles and at the end of the segment.  Each job
 // carries a tile ticket: the CTA whose merge completes the job's tiles
 // finalises that job (centroids = sums / masses into the other buffer of the
