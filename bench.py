@@ -15,11 +15,14 @@ JSON line keys (rank 0):
              copies centroids, labels and masses out
   roofline   HBM roofline of the fused kernel: algorithmic bytes per point-
              iteration = 4*d (points read once) + 4 (label written)
-  cpu_baseline  the oracle (a restatement of the reference's single-threaded
-             KmeansNaive) on a 2^22-point sample of the same workload
+  cpu_baseline  the reference's own KmeansNaive32 (compiled unchanged into
+             oracle/_ref; the oracle port where that build is absent) on a
+             2^22-point sample of the same workload, one thread
 
---impl reference runs the reference's CPU path (the oracle port, threaded
-over all host cores) on a bounded sample instead.
+--impl reference runs the reference's CPU path instead: its own KmeansNaive32
+compiled unchanged (oracle/_ref; single-threaded, as the reference is) on a
+bounded sample of the workload, with the oracle port threaded over all host
+cores beside it.
 """
 import argparse
 import ctypes
@@ -150,6 +153,38 @@ def cpu_port_rate(P, n, d, k, iters, threads):
     return n * iters / dt, dt
 
 
+def reference_cpu_available():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    return O.ref_available()
+
+
+def reference_cpu_rate(P, n, d, k, iters):
+    """pts*it/s of the reference's own KmeansNaive32 (kmeans_naive.cpp:31-106,
+    compiled unchanged into oracle/_ref), single-threaded as the reference is,
+    first-k initial centroids, timed over its iteration loop alone."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    C0 = O.first_x_f32(P, n, d, k)
+    _, _, _, loop_s = O.ref_naive_f32_timed(P, n, d, k, iters, C0)
+    return n * iters / loop_s, loop_s
+
+
+def cpu_baseline_record(P, n, d, k, iters, what):
+    """The CPU baseline of a bench line: the reference's own KmeansNaive32
+    when oracle/_ref was built on this machine, else the oracle port."""
+    if reference_cpu_available():
+        rate, dt = reference_cpu_rate(P, n, d, k, iters)
+        return {"value": rate, "unit": "pts*iter/s", "cores": 1, "host_cores": os.cpu_count(),
+                "kind": "reference",
+                "sample": "%s, %d iterations, %.1f s; KmeansNaive32 compiled unchanged, 1 of %d host cores"
+                          % (what, iters, dt, os.cpu_count() or 1)}
+    rate, dt = cpu_port_rate(P, n, d, k, iters, 1)
+    return {"value": rate, "unit": "pts*iter/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
+            "sample": "%s, %d iterations, %.1f s; oracle port (the reference build is absent on this machine)"
+                      % (what, iters, dt)}
+
+
 def host_sample(n_s, d, blobs, slo, shi):
     """A host-generated sample with the workload's distribution (numpy, same
     mixture parameters and seed), so the CPU arm touches no GPU code."""
@@ -179,42 +214,72 @@ def replica_throughput(units_per_rank, world, max_ms):
 
 
 def run_reference_arm(args, workload):
+    """The reference's own CPU implementation of the path: KmeansNaive32
+    (kmeans_naive.cpp:31-106) compiled unchanged into oracle/_ref, which is
+    single-threaded, so it runs on one of the host's cores.  One step = one
+    Lloyd iteration over a bounded sample of the workload (host-generated,
+    same mixture), the centroids carried from step to step; the value is the
+    sample's points x steps over the reference's own loop time.  The oracle
+    port threaded over all host cores is reported beside it."""
     n, d, k, blobs, slo, shi, iters_cfg = WORKLOADS[workload]
     rank = env_int("RANK", 0)
     if rank != 0:
         return 0
-    threads = os.cpu_count() or 1
-    # bounded sample of the workload, sized from a probe so the whole
-    # warmup + steps run stays within a couple of minutes
-    probe_n = 1 << 18
-    P = host_sample(1 << 22, d, blobs, slo, shi)
-    Pp = np.ascontiguousarray(P.reshape(d, -1)[:, :probe_n]).reshape(-1)
-    rate, _ = cpu_port_rate(Pp, probe_n, d, k, 2, threads)
-    budget_s = 90.0
-    per_step_pts = max(1 << 14, min(1 << 22, int(rate * budget_s / max(1, args.steps + args.warmup))))
-    n_s = 1 << int(np.floor(np.log2(per_step_pts)))
-    Ps = np.ascontiguousarray(P.reshape(d, -1)[:, :n_s]).reshape(-1)
+    host_cores = os.cpu_count() or 1
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    have_ref = O.ref_available()
+    # bounded sample, sized from a probe so warmup + steps take about a minute
+    probe_n = 1 << 18
+    P = host_sample(1 << 24, d, blobs, slo, shi)
+    Pp = np.ascontiguousarray(P.reshape(d, -1)[:, :probe_n]).reshape(-1)
+    if have_ref:
+        rate, _ = reference_cpu_rate(Pp, probe_n, d, k, 2)
+    else:
+        rate, _ = cpu_port_rate(Pp, probe_n, d, k, 2, 1)
+    budget_s = 60.0
+    per_step_pts = max(1 << 14, min(1 << 24, int(rate * budget_s / max(1, args.steps + args.warmup))))
+    n_s = 1 << int(np.floor(np.log2(per_step_pts)))
+    Ps = np.ascontiguousarray(P.reshape(d, -1)[:, :n_s]).reshape(-1)
     C = O.first_x_f32(Ps, n_s, d, k)
+
+    def one_step(C):
+        if have_ref:
+            C, _, _, loop_s = O.ref_naive_f32_timed(Ps, n_s, d, k, 1, C)
+            return C, loop_s
+        t0 = time.perf_counter()
+        C, _, _ = O.lloyd_f32(Ps, n_s, d, k, 1, C)
+        return C, time.perf_counter() - t0
+
     for _ in range(args.warmup):
-        C, _, _ = O.lloyd_f32_mt(Ps, n_s, d, k, 1, C, threads)
+        C, _ = one_step(C)
+    loop_s = 0.0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        C, _, _ = O.lloyd_f32_mt(Ps, n_s, d, k, 1, C, threads)
-    dt = time.perf_counter() - t0
-    value = n_s * args.steps / dt
+        C, dt = one_step(C)
+        loop_s += dt
+    wall = time.perf_counter() - t0
+    value = n_s * args.steps / loop_s
+    kind = "reference" if have_ref else "port"
+    impl = ("KmeansNaive32 (kmeans_naive.cpp) compiled unchanged (oracle/_ref), single-threaded" if have_ref else
+            "oracle port of KmeansNaive (the reference build is absent on this machine), single-threaded")
+    # the port threaded over every host core, one iteration on the same sample
+    Cp = O.first_x_f32(Ps, n_s, d, k)
+    tp = time.perf_counter()
+    O.lloyd_f32_mt(Ps, n_s, d, k, 1, Cp, host_cores)
+    port_mt = n_s / (time.perf_counter() - tp)
     line = {
         "impl": "reference", "metric": "pts*iter/s", "value": value, "unit": "pts*iter/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": loop_s / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded Gaussian mixture, sample of the workload)",
-        "config": {"workload": workload, "n": n, "d": d, "k": k, "sample_points": n_s,
-                   "implementation": "oracle port of the reference KmeansNaive (kmeans_naive.cpp), "
-                                     "labeling split over host threads"},
-        "cpu_baseline": {"value": value, "unit": "pts*iter/s", "cores": threads, "kind": "port",
-                         "sample": "%d points of the workload, 1 iteration per step" % n_s},
+        "data": "synthetic (seeded Gaussian mixture, host-generated sample of the workload)",
+        "config": {"workload": workload, "n": n, "d": d, "k": k, "sample_points": n_s, "implementation": impl},
+        "cpu_baseline": {"value": value, "unit": "pts*iter/s", "cores": 1, "host_cores": host_cores, "kind": kind,
+                         "sample": "%d points of the workload, 1 iteration per step, %d steps, %.1f s wall"
+                                   % (n_s, args.steps, wall)},
         "e2e": {"value": value, "unit": "pts*iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "port_threaded": {"value": port_mt, "unit": "pts*iter/s", "cores": host_cores,
+                          "call": "oracle port of KmeansNaive, labeling and sums split over host threads"},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -698,9 +763,7 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     if not args.no_cpu_baseline:
         n_s = 1 << 12
         Ps = np.ascontiguousarray(P.view(d, n)[:, :n_s].cpu().numpy()).reshape(-1)
-        rate, dt = cpu_port_rate(Ps, n_s, d, k, 1, 1)
-        cpu = {"value": rate, "unit": "pts*iter/s", "cores": 1, "kind": "port",
-               "sample": "first %d points, 1 iteration, %.1f s" % (n_s, dt)}
+        cpu = cpu_baseline_record(Ps, n_s, d, k, 1, "first %d points" % n_s)
     line = {
         "metric": "pts*iter/s", "value": n / step_s, "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
         "warmup": warm, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -908,9 +971,7 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         n_s, it_s = 1 << 22, iters_cfg
         Ps = np.ascontiguousarray(P.view(d, n)[:, :n_s].cpu().numpy()).reshape(-1)
-        rate, dt = cpu_port_rate(Ps, n_s, d, k, it_s, 1)
-        cpu = {"value": rate, "unit": "pts*iter/s", "cores": 1, "kind": "port",
-               "sample": "first %d points of the workload, %d iterations, %.1f s" % (n_s, it_s, dt)}
+        cpu = cpu_baseline_record(Ps, n_s, d, k, it_s, "first %d points of the workload" % n_s)
 
     if rank == 0:
         line = {

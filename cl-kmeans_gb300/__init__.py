@@ -559,6 +559,7 @@ class ServerResult(ctypes.Structure):
     """struct ckm_server_result (include/ckm.h)."""
     _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int), ("iterations", ctypes.c_uint32),
                 ("converged", ctypes.c_uint32), ("shift", ctypes.c_float), ("lane", ctypes.c_uint32),
+                ("first_round", ctypes.c_uint64), ("last_round", ctypes.c_uint64),
                 ("latency_ns", ctypes.c_uint64), ("error", ctypes.c_char * 128)]
 
 
@@ -624,7 +625,8 @@ class Server:
             r = arr[i]
             _, _, C, M, Lb = self._live.pop(r.tag)
             out.append(dict(tag=r.tag, status=r.status, iterations=r.iterations, converged=r.converged,
-                            shift=r.shift, lane=r.lane, latency_ns=r.latency_ns, error=r.error.decode(errors="replace"),
+                            shift=r.shift, lane=r.lane, first_round=r.first_round, last_round=r.last_round,
+                            latency_ns=r.latency_ns, error=r.error.decode(errors="replace"),
                             centroids=C, masses=M, labels=Lb))
         return out
 

@@ -22,10 +22,14 @@
 //   - the array keeps the previous call's contents, so each call clears the
 //     part it uses (one cudaMemsetAsync on the caller's stream) before the
 //     kernel runs.
-// Set-up: the first call on each device, with that device current, looks up
-// the array's device address (cudaGetSymbolAddress, which also loads this
-// module); later calls reuse it.  Make that first call before any stream
-// capture begins.
+// Set-up: the first call in each CUDA context (the first call on each device,
+// and the first one again after cudaDeviceReset or after a driver-API caller
+// made another context current) looks up the array's device address with
+// that device current (cudaGetSymbolAddress, which also loads this module);
+// later calls in the same context reuse it.  Make that first call before any
+// stream capture begins.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "ckm_internal.h"
@@ -42,23 +46,54 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 std::mutex g_mu;
 void* g_scratch_addr[MAX_DEVICES];
-bool g_scratch_ready[MAX_DEVICES];
+unsigned long long g_scratch_ctx[MAX_DEVICES];  // id of the context the address belongs to (0: none)
 
-// Device address of the built-in scratch for the current device (looked up
-// once per device).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Process-unique id of the current CUDA context (cuCtxGetId, reached through
+// the runtime's driver entry points, so the library needs no -lcuda); 0 when
+// no context is current or the entry points are unavailable.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_cur = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (!get_cur || !get_id) return 0;
+    CUcontext c = nullptr;
+    if (get_cur(&c) != CUDA_SUCCESS || !c) return 0;
+    unsigned long long id = 0;
+    return get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+// Device address of the built-in scratch in the current context: looked up
+// once per context (a cached address from a context that was reset or is not
+// current any more would point at memory this call does not own).
 int builtin_scratch(void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= MAX_DEVICES) return fail(CKM_ERR_UNSUPPORTED, "device ordinal out of range");
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> g(g_mu);
-    if (!g_scratch_ready[dev]) {
+    if (ctx == 0 || g_scratch_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(built-in scratch)");
         if (p == nullptr) return fail(CKM_ERR_CUDA, "built-in scratch has no device address");
         g_scratch_addr[dev] = p;
-        g_scratch_ready[dev] = true;
+        // the lookup made the device's primary context current if none was
+        g_scratch_ctx[dev] = ctx ? ctx : current_context_id();
     }
     *out = g_scratch_addr[dev];
     return CKM_OK;

@@ -59,6 +59,7 @@ struct SJob {
     unsigned long long* d_msum = nullptr;
     int slot = -1;
     uint64_t joined = 0;   // the first batched round the job is part of
+    uint64_t left = 0;     // the round whose status showed it stopped
 };
 
 // Byte layout of a small job's block.
@@ -139,6 +140,8 @@ void finish(ckm_server* S, SJob* j, int status, uint32_t its, uint32_t conv, flo
     r.converged = conv;
     r.shift = shift;
     r.lane = lane;
+    r.first_round = lane == 0 ? j->joined : 0;
+    r.last_round = lane == 0 ? j->left : 0;
     r.latency_ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - j->t_submit).count();
     std::memset(r.error, 0, sizeof(r.error));
     if (status != CKM_OK) {  // the lane's thread set the message
@@ -411,6 +414,7 @@ void small_lane(ckm_server* S) {
                     keep.push_back(j);
                     continue;
                 }
+                j->left = fl_id;
                 r.jobs.push_back(j);
                 r.status.push_back(b);
             }

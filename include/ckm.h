@@ -146,8 +146,9 @@ int ckm_unpermute_u32(uint64_t num_points, const uint32_t *perm, const uint32_t 
  * mode: CKM_MODE_FINALIZE or CKM_MODE_ACCUMULATE.  The array is shared by
  * all calls on a device: calls that may overlap on the GPU race, so keep
  * them on one stream.  Each call clears the part it uses first.  The first
- * call on a device looks up the array's address (cudaGetSymbolAddress);
- * make it before any stream capture. */
+ * call in each CUDA context (on each device, and again after cudaDeviceReset
+ * or a switch to another context) looks up the array's address
+ * (cudaGetSymbolAddress); make it before any stream capture. */
 int ckm_fused_f32_noalloc(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
                           const float *points, const float *old_centroids, float *new_centroids,
                           uint32_t *labels, uint32_t *masses, int mode, ckm_stream_t stream);
@@ -443,6 +444,8 @@ typedef struct ckm_server_result {
     uint32_t converged;            /* 1: stopped on the tolerance; 0: on the iteration cap */
     float shift;                   /* relative centroid shift of the last iteration */
     uint32_t lane;                 /* 0: batched lane; 1: large-job lane on the tensor cores; 2: large-job lane, SIMT */
+    uint64_t first_round;          /* batched lane: the first round (1, 2, ...) the job ran in; 0 otherwise */
+    uint64_t last_round;           /* batched lane: the round in which it stopped; 0 otherwise */
     uint64_t latency_ns;           /* submit -> results in the caller's host arrays */
     char error[128];               /* why the job failed (empty when status is CKM_OK) */
 } ckm_server_result;

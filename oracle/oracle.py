@@ -75,6 +75,8 @@ def ref():
         R = ctypes.CDLL(REF_SO)
         R.ckm_ref_naive_f32.argtypes = [_f32p, _u64, _u32, _u32, _u32, _f32p, _u32p, _u32p, ctypes.c_int]
         R.ckm_ref_naive_f64.argtypes = [_f64p, _u64, _u32, _u32, _u32, _f64p, _u64p, _u64p, ctypes.c_int]
+        R.ckm_ref_naive_f32_timed.argtypes = [_f32p, _u64, _u32, _u32, _u32, _f32p, _u32p, _u32p, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_uint64)]
         _ref = R
     return _ref
 
@@ -185,6 +187,18 @@ def ref_naive_f32(P, n, d, k, iterations, C0=None):
     lab = np.zeros(n, np.uint32)
     R.ckm_ref_naive_f32(P, n, d, k, iterations, C, m, lab, 1 if C0 is None else 0)
     return C, m, lab
+
+
+def ref_naive_f32_timed(P, n, d, k, iterations, C0):
+    """The reference's KmeansNaive32 from the given centroids; also returns the
+    seconds of its iteration loop alone (no Matrix copies)."""
+    R = ref()
+    C = np.array(C0, np.float32, copy=True)
+    m = np.zeros(k, np.uint32)
+    lab = np.zeros(n, np.uint32)
+    ns = ctypes.c_uint64(0)
+    R.ckm_ref_naive_f32_timed(P, n, d, k, iterations, C, m, lab, 0, ctypes.byref(ns))
+    return C, m, lab, ns.value / 1e9
 
 
 def ref_naive_f64(P, n, d, k, iterations, C0=None):

@@ -19,6 +19,7 @@ namespace Measurement { class Measurement {}; }
 #include "kmeans_naive.cpp"
 #include "kmeans_initializer.cpp"
 
+#include <chrono>
 #include <cstring>
 
 namespace {
@@ -32,7 +33,8 @@ cle::Matrix<T, std::allocator<T>, size_t, true> make_matrix(T const* data, size_
 
 template <typename PointT, typename LabelT, typename MassT>
 int run_naive(PointT const* points, uint64_t n, uint32_t d, uint32_t k, uint32_t iterations,
-              PointT* centroids, MassT* masses, LabelT* labels, int init_first_x) {
+              PointT* centroids, MassT* masses, LabelT* labels, int init_first_x,
+              uint64_t* loop_ns = nullptr) {
     auto P = make_matrix(points, n, d);
     cle::Matrix<PointT, std::allocator<PointT>, size_t, true> C;
     C.resize(k, d);
@@ -45,8 +47,12 @@ int run_naive(PointT const* points, uint64_t n, uint32_t d, uint32_t k, uint32_t
     std::vector<LabelT> L(n, 0);
     Clustering::KmeansNaive<PointT, LabelT, MassT> naive;
     naive.initialize();
+    auto t0 = std::chrono::steady_clock::now();
     naive(iterations, P, C, M, L);
+    auto t1 = std::chrono::steady_clock::now();
     naive.finalize();
+    if (loop_ns)
+        *loop_ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count();
     std::memcpy(centroids, &*C.begin(), sizeof(PointT) * k * d);
     std::memcpy(masses, M.data(), sizeof(MassT) * k);
     std::memcpy(labels, L.data(), sizeof(LabelT) * n);
@@ -64,6 +70,16 @@ int ckm_ref_naive_f32(float const* points, uint64_t n, uint32_t d, uint32_t k,
                       uint32_t* labels, int init_first_x) {
     return run_naive<float, uint32_t, uint32_t>(points, n, d, k, iterations, centroids,
                                                 masses, labels, init_first_x);
+}
+
+/* The same call, also returning the wall time of the KmeansNaive call alone
+ * (the iteration loop, kmeans_naive.cpp:31-106), without the copies into and
+ * out of the reference's Matrix type.  Timed CPU baseline of bench.py. */
+int ckm_ref_naive_f32_timed(float const* points, uint64_t n, uint32_t d, uint32_t k,
+                            uint32_t iterations, float* centroids, uint32_t* masses,
+                            uint32_t* labels, int init_first_x, uint64_t* loop_ns) {
+    return run_naive<float, uint32_t, uint32_t>(points, n, d, k, iterations, centroids,
+                                                masses, labels, init_first_x, loop_ns);
 }
 
 /* KmeansNaive64 (kmeans_naive.hpp:41-42). */

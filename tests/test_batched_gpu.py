@@ -144,7 +144,9 @@ def test_batch_convergence_stop(ckm, oracle, cuda):
             C = j["centroids"].cpu().numpy()
             L = j["labels"][:n].cpu().numpy().view(np.uint32)
             M = j["masses"].cpu().numpy().view(np.uint32)
-            _e2e_check(oracle, P, n, d, k, int(its[i]), C0, C, M, L)
+            it = int(its[i])
+            _e2e_check(oracle, P, n, d, k, it, C0, C, M, L,
+                       lambda: ckm.kmeans_run(P, d, k, it - 1, C0)[0], prev_slack_ulps=2)
     finally:
         b.close()
 

@@ -1,0 +1,139 @@
+"""Parity at the benchmark configurations' own sizes, against the oracle and
+an FP64 oracle.
+
+* Plain Lloyd, n = 2^20, d = 4, k = 10, 30 iterations (10 isotropic blobs,
+  centres U[-10, 10]^4, sigma 1, equal weights, shuffled from seed 42;
+  initial centroids the first k points, kmeans_initializer.cpp:29-39), end to
+  end through ckm_kmeans_run_f32 for the single-stage and three-stage
+  pipelines (kmeans_single_stage.hpp:52-172, kmeans_three_stage.hpp:66-243).
+  Labels against the oracle's FP32 KmeansNaive run (and the reference's own
+  build when present); every mismatch is adjudicated in FP64 against the
+  derived near-tie bound (tests/parity.py).  Centroids against an FP64
+  Lloyd run from the same start: relative error <= 1e-5.
+* HBM-scale Lloyd (n = 2^28, d = 4, k = 16, 16 blobs, sigma U[0.5, 2]): the
+  first 2^24 points of the same generated set in lockstep, on the caller's
+  order (ckm_fused_f32) and on the spatial order (ckm_spatial_sort_f32 +
+  ckm_fused_sorted_f32) -- every iteration's labels bit-exact against the
+  oracle from the same input centroids, masses exact, centroids within the
+  fused tolerance of the FP64 means; and the full 2^28 points through
+  size-independent properties: both orders give the same masses and
+  centroids, the masses sum to n, and a 2^20-point sample of the labels equals
+  the oracle's.
+"""
+import numpy as np
+import pytest
+
+import parity
+from conftest import blobs
+from test_fused_gpu import check_centroids
+
+pytestmark = pytest.mark.gpu
+
+FP64_REL_TOL = 1e-5
+
+
+@pytest.mark.parametrize("pipeline", ["single_stage", "three_stage"])
+def test_config1_end_to_end(ckm, oracle, cuda, pipeline):
+    n, d, k, iters = 1 << 20, 4, 10, 30
+    P = blobs(n, d, k, seed=42)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    C, M, L, info = ckm.kmeans_run(P, d, k, iters, C0, pipeline=pipeline)
+    assert info.iterations == iters
+    L = L.view(np.uint32)
+    Cr, Mr, Lr = oracle.lloyd_f32(P, n, d, k, iters, C0)
+    if oracle.ref_available():
+        # the oracle is the reference's arithmetic, bit for bit, at this size too
+        Cx, Mx, Lx = oracle.ref_naive_f32(P, n, d, k, iters, C0)
+        assert np.array_equal(Lx, Lr) and np.array_equal(Mx, Mr)
+        assert np.array_equal(Cx.view(np.uint32), Cr.view(np.uint32))
+
+    def ours_prev():
+        return ckm.kmeans_run(P, d, k, iters - 1, C0, pipeline=pipeline)[0]
+
+    prev = None
+    if np.any(L != Lr):
+        prev = ours_prev()
+        parity.adjudicate(P, n, d, k, L, Lr, prev, oracle.lloyd_f32(P, n, d, k, iters - 1, C0)[0])
+    assert np.array_equal(M, oracle.mass_u32(L, k))
+    check_centroids(oracle, P, n, d, k, L, C)
+
+    # against the FP64 oracle (FP64 distances and sums, the same FP32 points)
+    C64, M64, L64 = oracle.lloyd_fp64_of_f32(P, n, d, k, iters, C0)
+    if np.any(L != L64):
+        prev = ours_prev() if prev is None else prev
+        parity.adjudicate(P, n, d, k, L, L64, prev, oracle.lloyd_fp64_of_f32(P, n, d, k, iters - 1, C0)[0])
+    assert parity.rel_centroid_error(C, C64) <= FP64_REL_TOL
+
+
+def _c2a(ckm, cuda, n, first_point=0):
+    import torch
+    P = torch.empty(n * 4, dtype=torch.float32, device=cuda)
+    ckm.generate_mixture(P, n, 4, 16, 42, sigma=(0.5, 2.0), first_point=first_point)
+    return P
+
+
+@pytest.mark.parametrize("order", ["caller", "spatial"])
+def test_config2a_lockstep_2p24(ckm, oracle, cuda, order):
+    import torch
+    n, d, k, iters = 1 << 24, 4, 16, 4
+    dP = _c2a(ckm, cuda, n)
+    P = dP.cpu().numpy()
+    C = [dP.view(d, n)[:, :k].reshape(-1).clone(), torch.empty(k * d, dtype=torch.float32, device=cuda)]
+    dL = torch.empty(n, dtype=torch.int32, device=cuda)
+    dM = torch.empty(k, dtype=torch.int32, device=cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    if order == "spatial":
+        dPs, perm = ckm.spatial_sort(dP, n, d)
+        torch.cuda.synchronize()
+        perm_h = perm.cpu().numpy().view(np.uint32)
+        assert np.array_equal(np.sort(perm_h), np.arange(n, dtype=np.uint32))
+        assert np.array_equal(dPs.cpu().numpy().reshape(d, n), P.reshape(d, n)[:, perm_h])
+    for it in range(iters):
+        Cin = C[it % 2].cpu().numpy()
+        if order == "spatial":
+            ckm.fused_sorted(dPs, C[it % 2], C[(it + 1) % 2], dL, dM, S, n, d, k, ckm.MODE_FINALIZE)
+        else:
+            ckm.fused(dP, C[it % 2], C[(it + 1) % 2], dL, dM, S, n, d, k, ckm.MODE_FINALIZE)
+        torch.cuda.synchronize()
+        ref = oracle.label_f32(P, n, d, k, Cin)
+        L = dL.cpu().numpy().view(np.uint32)
+        assert np.array_equal(L, ref[perm_h] if order == "spatial" else ref), "iteration %d" % it
+        assert np.array_equal(dM.cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+        check_centroids(oracle, P, n, d, k, ref, C[(it + 1) % 2].cpu().numpy())
+
+
+def test_config2a_full_size_properties(ckm, oracle, cuda):
+    """n = 2^28: one iteration on each order from the first-k centroids."""
+    import torch
+    n, d, k = 1 << 28, 4, 16
+    dP = _c2a(ckm, cuda, n)
+    C0 = dP.view(d, n)[:, :k].reshape(-1).clone()
+    out = {}
+    dL = torch.empty(n, dtype=torch.int32, device=cuda)
+    dM = torch.empty(k, dtype=torch.int32, device=cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    Cn = torch.empty(k * d, dtype=torch.float32, device=cuda)
+    ckm.fused(dP, C0, Cn, dL, dM, S, n, d, k, ckm.MODE_FINALIZE)
+    torch.cuda.synchronize()
+    out["caller"] = (dM.cpu().numpy().view(np.uint32).copy(), Cn.cpu().numpy().copy())
+    rng = np.random.default_rng(7)
+    sample = np.sort(rng.choice(n, size=1 << 20, replace=False))
+    Xs = np.ascontiguousarray(dP.view(d, n)[:, torch.from_numpy(sample).to(cuda)].cpu().numpy()).reshape(-1)
+    ref_sample = oracle.label_f32(Xs, len(sample), d, k, C0.cpu().numpy())
+    assert np.array_equal(dL.cpu().numpy().view(np.uint32)[sample], ref_sample)
+    dPs, perm = ckm.spatial_sort(dP, n, d)
+    del dP
+    ckm.fused_sorted(dPs, C0, Cn, dL, dM, S, n, d, k, ckm.MODE_FINALIZE)
+    torch.cuda.synchronize()
+    out["spatial"] = (dM.cpu().numpy().view(np.uint32).copy(), Cn.cpu().numpy().copy())
+    Ls = torch.empty_like(dL)
+    ckm.unpermute(perm, dL, Ls, n)
+    torch.cuda.synchronize()
+    assert np.array_equal(Ls.cpu().numpy().view(np.uint32)[sample], ref_sample)
+    m_c, c_c = out["caller"]
+    m_s, c_s = out["spatial"]
+    assert int(m_c.astype(np.uint64).sum()) == n
+    assert np.array_equal(m_c, m_s)
+    # the same labels: the FP64-merged sums of the two orders round to FP32 at
+    # most one ulp apart
+    assert np.all(np.abs(c_c - c_s) <= np.spacing(np.abs(c_c)))

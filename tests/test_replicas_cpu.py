@@ -66,9 +66,10 @@ def test_single_rank_is_its_own_time():
 
 
 def test_reference_arm_line_on_the_cpu():
-    """bench.py --impl reference times the reference's CPU path (the oracle
-    port of KmeansNaive) on the host cores and prints one JSON line with the
-    contract's keys; it needs no GPU."""
+    """bench.py --impl reference times the reference's CPU path (its own
+    KmeansNaive32 compiled unchanged into oracle/_ref, single-threaded; the
+    oracle port only where that build is absent) and prints one JSON line with
+    the contract's keys; it needs no GPU."""
     import json
     import subprocess
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
@@ -81,6 +82,10 @@ def test_reference_arm_line_on_the_cpu():
     assert line["higher_is_better"] is True and line["warmup"] >= 3
     cpu = line["cpu_baseline"]
     assert cpu["kind"] in ("port", "reference") and cpu["cores"] >= 1 and cpu["sample"]
+    import oracle as O
+    if O.ref_available():
+        assert cpu["kind"] == "reference" and cpu["cores"] == 1
+    assert line["port_threaded"]["cores"] >= 1 and line["port_threaded"]["value"] > 0
     assert cpu["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}

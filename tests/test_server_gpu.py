@@ -8,6 +8,7 @@ fused tolerance of the FP64 means of the labels."""
 import numpy as np
 import pytest
 
+import parity
 from conftest import blobs
 from test_pipelines_gpu import _e2e_check
 
@@ -23,7 +24,7 @@ def _jobs(oracle, shapes, seed):
     return out
 
 
-def _check(oracle, job, res, tol, cap):
+def _check(ckm, oracle, job, res, tol, cap):
     P, C0, n, d, k = job
     assert res["status"] == 0
     its = res["iterations"]
@@ -32,7 +33,8 @@ def _check(oracle, job, res, tol, cap):
         assert res["shift"] < tol
     else:
         assert its == cap
-    _e2e_check(oracle, P, n, d, k, its, C0, res["centroids"], res["masses"], res["labels"])
+    _e2e_check(oracle, P, n, d, k, its, C0, res["centroids"], res["masses"], res["labels"],
+               lambda: ckm.kmeans_run(P, d, k, its - 1, C0)[0], prev_slack_ulps=2)
 
 
 def test_server_batched_lane_matches_single_runs(ckm, oracle, cuda):
@@ -50,7 +52,71 @@ def test_server_batched_lane_matches_single_runs(ckm, oracle, cuda):
         assert all(r["lane"] == 0 for r in res)
         assert any(r["converged"] for r in res)
         for r in res:
-            _check(oracle, jobs[r["tag"]], r, tol, cap)
+            _check(ckm, oracle, jobs[r["tag"]], r, tol, cap)
+    finally:
+        S.close()
+
+
+def test_server_continuous_batching(ckm, oracle, cuda):
+    """Jobs that arrive while rounds are on the GPU join a later round and run
+    beside the jobs already there, and each result is the same as the job's
+    run alone.
+
+    The first wave is long-running work (uniform points, no cluster
+    structure, so Lloyd creeps on for the whole 50-iteration cap at one
+    iteration per round); it is checked for completion only.  The second wave
+    arrives once two rounds have run; its jobs are Gaussian blobs started from
+    their blob centres, so no point sits near a tie and the run alone must
+    give the same labels and masses exactly and centroids within 1e-5
+    relative, and the oracle's run of the same length agrees as well."""
+    import time
+    tol, cap = 1e-6, 50
+
+    def uniform_job(n, d, k, seed):
+        P = np.ascontiguousarray(np.random.default_rng(seed).uniform(-5, 5, size=(d, n)).astype(np.float32)).reshape(-1)
+        return P, oracle.first_x_f32(P, n, d, k), n, d, k
+
+    def blob_job(n, d, k, seed):
+        rng = np.random.default_rng(seed)
+        centres = rng.uniform(-10, 10, size=(k, d))
+        X = centres[rng.integers(0, k, size=n)] + rng.standard_normal((n, d))
+        P = np.ascontiguousarray(X.astype(np.float32).T).reshape(-1)
+        C0 = np.ascontiguousarray((centres + 0.1 * rng.standard_normal((k, d))).astype(np.float32).T).reshape(-1)
+        return P, C0, n, d, k
+
+    rng = np.random.default_rng(4)
+    wave1 = [uniform_job(1 << 17, 32, 64, 100 + i) for i in range(12)]
+    wave2 = [blob_job(int(rng.integers(2000, 20000)), int(rng.choice([2, 4, 16])), int(rng.integers(3, 12)), 200 + i)
+             for i in range(12)]
+    S = ckm.Server(tolerance=tol, max_iterations=cap, round_iterations=1)
+    try:
+        for t, (P, C0, n, d, k) in enumerate(wave1):
+            S.submit(P, C0, n, d, k, tag=t)
+        t0 = time.perf_counter()
+        while S.stats()["rounds"] < 2:
+            assert time.perf_counter() - t0 < 30, "the server ran no round"
+            time.sleep(0.0005)
+        rounds_at_submit = S.stats()["rounds"]
+        for t, (P, C0, n, d, k) in enumerate(wave2):
+            S.submit(P, C0, n, d, k, tag=100 + t)
+        S.drain()
+        res = {r["tag"]: r for r in S.poll()}
+        assert sorted(res) == list(range(len(wave1))) + [100 + t for t in range(len(wave2))]
+        assert all(r["status"] == 0 and r["lane"] == 0 for r in res.values())
+        first2 = min(res[100 + t]["first_round"] for t in range(len(wave2)))
+        # the late jobs joined rounds after those already launched ...
+        assert all(res[100 + t]["first_round"] > rounds_at_submit for t in range(len(wave2)))
+        assert all(res[t]["first_round"] >= 1 for t in range(len(wave1)))
+        # ... while jobs of the first wave were still running beside them
+        assert max(res[t]["last_round"] for t in range(len(wave1))) >= first2
+        for t, job in enumerate(wave2):
+            r = res[100 + t]
+            _check(ckm, oracle, job, r, tol, cap)
+            P, C0, n, d, k = job
+            Ca, Ma, La, _ = ckm.kmeans_run(P, d, k, r["iterations"], C0)
+            assert np.array_equal(La.view(np.uint32), r["labels"])
+            assert np.array_equal(Ma, r["masses"])
+            assert parity.rel_centroid_error(r["centroids"], Ca) <= 1e-5
     finally:
         S.close()
 
@@ -72,7 +138,7 @@ def test_server_large_lane(ckm, oracle, cuda):
         assert res[0]["lane"] == want_tc and res[1]["lane"] == 2
         assert res[2]["lane"] == 0 and res[3]["lane"] == 0
         for t, r in res.items():
-            _check(oracle, jobs[t], r, tol, cap)
+            _check(ckm, oracle, jobs[t], r, tol, cap)
     finally:
         S.close()
 

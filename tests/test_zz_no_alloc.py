@@ -60,6 +60,10 @@ def test_noalloc_two_calls_match_scratch_entry_point(ckm, oracle, cuda):
         ref = _run(ckm, cuda, P, n, d, k, C, noalloc=False)
         got = _run(ckm, cuda, P, n, d, k, C, noalloc=True)
         _same(ref, got, float(np.abs(P).max()))
+        # and directly against the oracle: the reference's labels and masses
+        want = oracle.label_f32(P, n, d, k, C)
+        assert np.array_equal(got[2].view(np.uint32), want)
+        assert np.array_equal(got[1].view(np.uint32), oracle.mass_u32(want, k))
 
 
 def test_noalloc_repeated_calls_and_accumulate_mode(ckm, oracle, cuda):
@@ -73,6 +77,31 @@ def test_noalloc_repeated_calls_and_accumulate_mode(ckm, oracle, cuda):
     refA = _run(ckm, cuda, P, n, d, k, C, noalloc=False, mode=2, acc_init=(0.5, 7))
     gotA = _run(ckm, cuda, P, n, d, k, C, noalloc=True, mode=2, acc_init=(0.5, 7))
     _same(refA, gotA, float(np.abs(P).max()) * 1000)
+
+
+def test_noalloc_allocates_nothing_after_setup(ckm, oracle, cuda):
+    """After the first call (set-up: the array's address, the kernels'
+    module), further calls leave the device's free memory and torch's
+    allocator untouched: no cudaMalloc, no allocating library routine."""
+    import torch
+    shapes = [(60000, 4, 16, 5), (20000, 20, 12, 6)]     # low-d and generic kernels
+    bufs = []
+    for n, d, k, seed in shapes:
+        P = blobs(n, d, k, seed=seed)
+        C = oracle.first_x_f32(P, n, d, k)
+        bufs.append((torch.from_numpy(P).to(cuda), torch.from_numpy(C).to(cuda),
+                     torch.zeros(k * d, dtype=torch.float32, device=cuda), torch.zeros(n, dtype=torch.int32, device=cuda),
+                     torch.zeros(k, dtype=torch.int32, device=cuda), n, d, k))
+    for dP, dC, dN, dL, dM, n, d, k in bufs:            # set-up calls
+        ckm.fused_noalloc(dP, dC, dN, dL, dM, n, d, k)
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for _ in range(5):
+        for dP, dC, dN, dL, dM, n, d, k in bufs:
+            ckm.fused_noalloc(dP, dC, dN, dL, dM, n, d, k)
+    torch.cuda.synchronize()
+    assert torch.cuda.memory_allocated() == alloc0
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_noalloc_rejects_sizes_beyond_builtin_scratch(ckm, cuda):
