@@ -71,19 +71,16 @@ def measured_hbm_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic_per_point(workload, key="dram_bytes_per_point"):
-    """DRAM bytes per point-iteration from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "fused_lowd_d4_k16.md")
-    if not os.path.exists(p):
+def profiled_traffic_per_point(key):
+    """DRAM bytes per point-iteration of the fused kernel from the committed
+    ncu summary's data file (profiles/fused_lowd_d4_k16.traffic.json), if any."""
+    p = os.path.join(ROOT, "profiles", "fused_lowd_d4_k16.traffic.json")
+    try:
+        with open(p) as f:
+            v = json.load(f).get(key)
+        return float(v) if v is not None else None
+    except (OSError, ValueError):
         return None
-    with open(p) as f:
-        for line in f:
-            if line.strip().startswith(key + ":"):
-                try:
-                    return float(line.split(":", 1)[1].strip())
-                except ValueError:
-                    return None
-    return None
 
 
 class ClockSampler:
@@ -183,6 +180,58 @@ def cpu_baseline_record(P, n, d, k, iters, what):
     return {"value": rate, "unit": "pts*iter/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
             "sample": "%s, %d iterations, %.1f s; oracle port (the reference build is absent on this machine)"
                       % (what, iters, dt)}
+
+
+def oracle_module():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    return O
+
+
+def rel_err(C, R):
+    """Normwise relative error max |C - R| / max |R| over entries finite in
+    both (NaN marks an empty cluster)."""
+    C = np.asarray(C, np.float64)
+    R = np.asarray(R, np.float64)
+    ok = np.isfinite(C) & np.isfinite(R)
+    if not ok.any():
+        return 0.0
+    return float(np.abs(C[ok] - R[ok]).max() / max(float(np.abs(R[ok]).max()), 1e-300))
+
+
+def fp64_means_check(P, n, d, k, labels, centroids, masses=None):
+    """Centroids against the FP64 means of the same labels (the oracle's FP64
+    sums), and whether the masses are the label counts."""
+    O = oracle_module()
+    sums, m64 = O.sums_f64(P, n, d, k, np.ascontiguousarray(labels, np.uint32))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ref = sums / np.tile(m64.astype(np.float64), d)
+    out = {"max_rel_centroid_err_vs_fp64_means": rel_err(centroids, ref)}
+    if masses is not None:
+        out["masses_equal_label_counts"] = bool(np.array_equal(np.asarray(masses, np.uint64), m64))
+    return out
+
+
+def fp64_label_check(Xs, m, d, k, C_in, ours):
+    """Labels of m sample points (column-major Xs) against the oracle's FP32
+    labels (bit-exact expected) and its FP64 labels; a disagreement with FP64
+    is explained when our label's FP64 distance exceeds the best one by no
+    more than the FP32 distance rounding allows, (d + 4) 2^-24 relative."""
+    O = oracle_module()
+    ref32 = O.label_f32(Xs, m, d, k, C_in)
+    lab64, _, _ = O.label_gap_f64(Xs, m, d, k, C_in)
+    ours = np.asarray(ours, np.uint32)
+    bad = np.nonzero(ours != lab64)[0]
+    explained = 0
+    if bad.size:
+        X = np.asarray(Xs, np.float64).reshape(d, m)[:, bad].T
+        Cr = np.asarray(C_in, np.float64).reshape(d, k).T
+        Da = ((X - Cr[ours[bad]]) ** 2).sum(1)
+        Db = ((X - Cr[lab64[bad]]) ** 2).sum(1)
+        rho = (d + 4) * 2.0 ** -24
+        explained = int(np.sum(Da - Db <= 2 * rho / (1 - rho) * Db + 1e-30))
+    return {"sample_points": int(m), "label_mismatches_vs_fp32_oracle": int(np.sum(ours != ref32)),
+            "label_mismatches_vs_fp64": int(bad.size), "fp64_mismatches_within_fp32_rounding": explained}
 
 
 def host_sample(n_s, d, blobs, slo, shi):
@@ -306,29 +355,15 @@ def make_batched_jobs(ckm, torch, num_jobs, seed_base, dev):
     return jobs
 
 
-def run_batched_workload(args, ckm, torch, dev):
+def batched_record(ckm, torch, dev, num_jobs, steps, warmup, fp64=True):
     """Batched uneven jobs: every job 20 fixed iterations, all jobs advanced by
     one persistent launch per iteration (CUDA graph), against the plain
     per-job loop (each job: its own fused launch per iteration) on the same
-    GPU.  Metric: jobs/s."""
-    num_jobs, iters = args.jobs, 20
+    GPU.  Metric: jobs/s.  Returns the record."""
+    iters = 20
     jobs = make_batched_jobs(ckm, torch, num_jobs, 1234, dev)
-    subset = None
-    if args.batch_d or args.batch_min_k or args.batch_max_k or args.batch_max_jobs:
-        # a class of the same job list (profiling and breakdowns)
-        jobs = [j for j in jobs if (not args.batch_d or j["d"] == args.batch_d) and j["k"] >= args.batch_min_k
-                and (not args.batch_max_k or j["k"] < args.batch_max_k)]
-        if args.batch_max_jobs:
-            jobs = jobs[:args.batch_max_jobs]
-        num_jobs = len(jobs)
-        subset = {"d": args.batch_d or None, "min_k": args.batch_min_k, "max_k": args.batch_max_k or None,
-                  "of_jobs": args.jobs}
-        torch.cuda.empty_cache()
     total_pts = sum(j["n"] for j in jobs)
     stream = torch.cuda.current_stream()
-    if args.no_plain:
-        return run_batched_only(args, ckm, torch, jobs, iters, total_pts, subset, stream)
-
     # plain per-job loop (the reference's one-problem-at-a-time structure):
     # ckm_fused_f32 per job and iteration, called through the raw C ABI with
     # the pointers prepared once, so the loop's cost is the per-job call and
@@ -371,15 +406,16 @@ def run_batched_workload(args, ckm, torch, dev):
         j["centroids"].copy_(j["init"])
     batch = ckm.Batch(jobs, autotune=True)
     info = batch.info()
-    for j in jobs:
-        j["centroids"].copy_(j["init"])
-    warm = max(3, args.warmup)
+    warm = max(3, warmup)
     for _ in range(warm):                 # capture + warm-up
         for j in jobs:
             j["centroids"].copy_(j["init"])
         batch.run(iters, use_graph=True)
     times = []
-    for _ in range(max(3, args.steps if args.steps < 20 else 5)):
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    for _ in range(max(3, steps if steps < 20 else 5)):
         for j in jobs:
             j["centroids"].copy_(j["init"])
         torch.cuda.synchronize()
@@ -391,24 +427,38 @@ def run_batched_workload(args, ckm, torch, dev):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
         gpu_launches = ckm.launch_count() - launches0
+    clocks = sampler.stop()
     batch_s = statistics.median(times)
-    # agreement with the plain loop (same arithmetic; FP64-merged sums)
-    worst = 0.0
+    # agreement with the plain loop after 20 iterations (same arithmetic;
+    # FP64-merged sums in another order)
+    worst, diverged = 0.0, 0
     for j, ref in zip(jobs, plain_result):
-        a, b = j["centroids"].cpu().numpy(), ref.cpu().numpy()
-        ok = ~(np.isnan(a) | np.isnan(b))
-        if ok.any():
-            scale = max(float(np.abs(b[ok]).max()), 1e-30)
-            worst = max(worst, float(np.abs(a[ok] - b[ok]).max()) / scale)
-    diverged = 0
-    for j, ref in zip(jobs, plain_result):
-        a, b = j["centroids"].cpu().numpy(), ref.cpu().numpy()
-        ok = ~(np.isnan(a) | np.isnan(b))
-        if ok.any() and np.abs(a[ok] - b[ok]).max() > 1e-5 * max(float(np.abs(b[ok]).max()), 1e-30):
-            diverged += 1
+        e = rel_err(j["centroids"].cpu().numpy(), ref.cpu().numpy())
+        worst = max(worst, e)
+        diverged += e > 1e-5
+    fp64_e2e = None
+    if fp64:
+        # 20 iterations end to end against the FP64 oracle (FP64 distances and
+        # sums on the same FP32 points, the same start), on the jobs small
+        # enough for the CPU; the oracle's own FP32 run (the reference's
+        # arithmetic) beside it shows how far FP32 Lloyd itself drifts
+        O = oracle_module()
+        small = [i for i, j in enumerate(jobs) if j["n"] * j["k"] * j["d"] <= (1 << 20)][:32]
+        errs, ref_errs = [], []
+        for i in small:
+            j = jobs[i]
+            Ph = j["points"].cpu().numpy()
+            C64, _, _ = O.lloyd_fp64_of_f32(Ph, j["n"], j["d"], j["k"], iters, j["init"].cpu().numpy())
+            C32, _, _ = O.lloyd_f32(Ph, j["n"], j["d"], j["k"], iters, j["init"].cpu().numpy())
+            errs.append(rel_err(j["centroids"].cpu().numpy(), C64))
+            ref_errs.append(rel_err(C32, C64))
+        fp64_e2e = {"jobs": len(small), "max_rel_centroid_err": max(errs) if errs else None,
+                    "jobs_within_1e-5": int(sum(e <= 1e-5 for e in errs)),
+                    "reference_fp32_max_rel_err": max(ref_errs) if ref_errs else None,
+                    "reference_fp32_jobs_within_1e-5": int(sum(e <= 1e-5 for e in ref_errs)),
+                    "selection": "jobs with n*k*d <= 2^20 (the first 32)"}
     # lockstep: one iteration of every job from the same centroids, batched
-    # against the plain fused call (the per-iteration agreement; after 20
-    # iterations a near-tie flip can send a job down another trajectory)
+    # against the plain fused call and against the FP64 oracle
     for j in jobs:
         j["centroids"].copy_(j["init"])
     batch.run(1, use_graph=False)
@@ -420,26 +470,67 @@ def run_batched_workload(args, ckm, torch, dev):
         ckm.fused(j["points"], j["init"], a, lab, mas, scratch[key], j["n"], j["d"], j["k"], ckm.MODE_FINALIZE, stream)
         torch.cuda.synchronize()
         lock_label_diff += int((lab != j["labels"]).sum().item())
-        x, y = j["centroids"].cpu().numpy(), a.cpu().numpy()
-        ok = ~(np.isnan(x) | np.isnan(y))
-        if ok.any():
-            lock_worst = max(lock_worst, float(np.abs(x[ok] - y[ok]).max()) / max(float(np.abs(y[ok]).max()), 1e-30))
+        lock_worst = max(lock_worst, rel_err(j["centroids"].cpu().numpy(), a.cpu().numpy()))
+    lock64 = None
+    if fp64:
+        O = oracle_module()
+        sample = list(range(0, len(jobs), max(1, len(jobs) // 256)))
+        worst64, masses_ok, lab_mis, lab_jobs = 0.0, True, 0, 0
+        for i in sample:
+            j = jobs[i]
+            Ph = j["points"].cpu().numpy()
+            labels = j["labels"].cpu().numpy().view(np.uint32)
+            r = fp64_means_check(Ph, j["n"], j["d"], j["k"], labels, j["centroids"].cpu().numpy(),
+                                 j["masses"].cpu().numpy().view(np.uint32))
+            worst64 = max(worst64, r["max_rel_centroid_err_vs_fp64_means"])
+            masses_ok &= r["masses_equal_label_counts"]
+            if j["n"] * j["k"] * j["d"] <= (1 << 23) and lab_jobs < 64:
+                lab_jobs += 1
+                lab_mis += int(np.sum(O.label_f32(Ph, j["n"], j["d"], j["k"], j["init"].cpu().numpy()) != labels))
+        lock64 = {"jobs": len(sample), "max_rel_centroid_err_vs_fp64_means": worst64,
+                  "within_1e-5": bool(worst64 <= 1e-5), "masses_equal_label_counts": bool(masses_ok),
+                  "label_mismatches_vs_fp32_oracle": lab_mis, "label_checked_jobs": lab_jobs}
     batch.close()
-    line = {
+    flops = sum(2.0 * j["n"] * j["k"] * j["d"] for j in jobs) * iters
+    algo_bytes = sum(float(j["n"]) * (4 * j["d"] + 4) for j in jobs) * iters
+    peak, peak_kind = measured_hbm_peak()
+    achieved = algo_bytes / batch_s / 1e9
+    return {
         "metric": "jobs/s", "value": num_jobs / batch_s, "unit": "jobs/s", "n_gpus": 1, "steps": len(times),
         "warmup": warm, "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (per-job seeded Gaussian mixtures generated on the device)",
         "config": {"workload": "batched_%d_jobs" % num_jobs, "iterations": iters, "total_points": total_pts,
                    "schedule": info, "graph": True},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "algorithmic_bytes_per_step": algo_bytes},
+        "tflops_exact_equivalent": flops / batch_s / 1e12,
         "plain_per_job_loop": {"jobs_per_s": num_jobs / plain_s, "seconds": plain_s,
                                "launches": num_jobs * iters},
         "speedup_vs_plain_loop": plain_s / batch_s,
         "pts_iter_per_s": total_pts * iters / batch_s,
         "lockstep_vs_plain": {"max_rel_centroid_diff": lock_worst, "label_mismatches": lock_label_diff},
-        "after_20_iterations_vs_plain": {"max_rel_centroid_diff": worst, "jobs_beyond_1e-5": diverged},
-        "gpu_launches": int(gpu_launches),
+        "lockstep_vs_fp64": lock64,
+        "after_20_iterations_vs_plain": {"max_rel_centroid_diff": worst, "jobs_beyond_1e-5": int(diverged)},
+        "after_20_iterations_vs_fp64": fp64_e2e,
+        "gpu_launches": int(gpu_launches), "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_batched_workload(args, ckm, torch, dev):
+    if args.batch_d or args.batch_min_k or args.batch_max_k or args.batch_max_jobs or args.no_plain:
+        # a class of the same job list (profiling and breakdowns): the
+        # batched launches alone
+        jobs = make_batched_jobs(ckm, torch, args.jobs, 1234, dev)
+        jobs = [j for j in jobs if (not args.batch_d or j["d"] == args.batch_d) and j["k"] >= args.batch_min_k
+                and (not args.batch_max_k or j["k"] < args.batch_max_k)]
+        if args.batch_max_jobs:
+            jobs = jobs[:args.batch_max_jobs]
+        subset = {"d": args.batch_d or None, "min_k": args.batch_min_k, "max_k": args.batch_max_k or None,
+                  "of_jobs": args.jobs}
+        torch.cuda.empty_cache()
+        return run_batched_only(args, ckm, torch, jobs, 20, sum(j["n"] for j in jobs), subset,
+                                torch.cuda.current_stream())
+    print(json.dumps(batched_record(ckm, torch, dev, args.jobs, args.steps, args.warmup)), flush=True)
     return 0
 
 
@@ -553,21 +644,23 @@ def measured_bf16_peak():
     return 1900.0, "fallback"
 
 
-def run_serving_workload(args, ckm, torch, dev):
+def serving_record(ckm, torch, dev, seconds, rate, large_rate, pool_size, plain_jobs, round_iterations,
+                   with_70pct=True, burst_rounds=4, fp64=True):
     """Served stream (config 5, scaled to what one GB300 and its host link
     carry): Poisson arrivals of config-4-shaped jobs (n log-U[2^10, 2^18],
-    d in {2, 8, 32, 64}, k log-U[4, 256], k <= n/16) at --serve-rate jobs/s
-    for --serve-seconds, plus large jobs (n = 2^22, d = 128, k = 1024) at
-    --serve-large-rate jobs/s; every job stops at relative centroid shift
-    < 1e-4 or 50 iterations.  Payloads come from pools generated once and held
-    in pinned host memory.  Reports throughput and p50/p99 latency under the
-    stream, the burst capacity of the batched lane, and a plain per-job loop
-    (ckm_kmeans_run with convergence, one job at a time) on the same jobs."""
+    d in {2, 8, 32, 64}, k log-U[4, 256], k <= n/16) at `rate` jobs/s for
+    `seconds`, plus large jobs (n = 2^22, d = 128, k = 1024) at `large_rate`
+    jobs/s; every job stops at relative centroid shift < 1e-4 or 50
+    iterations.  Payloads come from pools generated once and held in pinned
+    host memory.  Reports throughput and p50/p99 latency under the stream,
+    the burst capacity of the batched lane, and a plain per-job loop
+    (ckm_kmeans_run with convergence, one job at a time) on the same jobs.
+    Returns the record."""
     rng = np.random.default_rng(2024)
     tol, cap = 1e-4, 50
     # small-job pool
     pool = []
-    for i in range(args.serve_pool):
+    for i in range(pool_size):
         n = int(round(np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 18)))))
         d = int(rng.choice([2, 8, 32, 64]))
         k = int(round(np.exp(rng.uniform(np.log(4), np.log(256)))))
@@ -580,7 +673,7 @@ def run_serving_workload(args, ckm, torch, dev):
         pool.append((hp, hp.numpy(), C0, n, d, k))
         del P
     large = []
-    if args.serve_large_rate > 0:
+    if large_rate > 0:
         for i in range(2):
             n, d, k = 1 << 22, 128, 1024
             P = torch.empty(n * d, dtype=torch.float32, device=dev)
@@ -613,7 +706,7 @@ def run_serving_workload(args, ckm, torch, dev):
                 break
             arrivals.append((t, 1))
         arrivals.sort()
-        S = ckm.Server(tolerance=tol, max_iterations=cap, large_work=1 << 33, round_iterations=args.serve_round)
+        S = ckm.Server(tolerance=tol, max_iterations=cap, large_work=1 << 33, round_iterations=round_iterations)
         results = []
         t0 = time.perf_counter()
         for i, (ta, kind) in enumerate(arrivals):
@@ -637,17 +730,19 @@ def run_serving_workload(args, ckm, torch, dev):
         lat_l = np.array([r["latency_ns"] for r in ok if r["lane"] != 0]) / 1e6
         its = np.array([r["iterations"] for r in ok if r["lane"] == 0])
         pct = lambda a, q: float(np.percentile(a, q)) if a.size else None
-        return {"offered_small_per_s": lam, "offered_large_per_s": lam_l, "seconds": T, "offered_jobs": len(arrivals),
-                "completed_ok": len(ok), "failed": len(results) - len(ok), "jobs_per_s": len(ok) / t_end,
-                "latency_ms_small": {"p50": pct(lat_s, 50), "p99": pct(lat_s, 99)},
-                "latency_ms_large": {"p50": pct(lat_l, 50), "p99": pct(lat_l, 99), "count": int(lat_l.size)},
-                "iterations_small_mean": float(its.mean()) if its.size else None,
-                "converged_fraction_small": float(np.mean([r["converged"] for r in ok if r["lane"] == 0]))
-                if its.size else None}
+        summary = {"offered_small_per_s": lam, "offered_large_per_s": lam_l, "seconds": T,
+                   "offered_jobs": len(arrivals), "completed_ok": len(ok), "failed": len(results) - len(ok),
+                   "jobs_per_s": len(ok) / t_end,
+                   "latency_ms_small": {"p50": pct(lat_s, 50), "p99": pct(lat_s, 99)},
+                   "latency_ms_large": {"p50": pct(lat_l, 50), "p99": pct(lat_l, 99), "count": int(lat_l.size)},
+                   "iterations_small_mean": float(its.mean()) if its.size else None,
+                   "converged_fraction_small": float(np.mean([r["converged"] for r in ok if r["lane"] == 0]))
+                   if its.size else None}
+        return summary, ok
 
-    # 2. burst capacity of the batched lane: the whole small pool, 4 times over, at once
-    S = ckm.Server(tolerance=tol, max_iterations=cap, large_work=1 << 33, round_iterations=args.serve_round)
-    nb = 4 * len(pool)
+    # burst capacity of the batched lane: the whole small pool, several times over, at once
+    S = ckm.Server(tolerance=tol, max_iterations=cap, large_work=1 << 33, round_iterations=round_iterations)
+    nb = burst_rounds * len(pool)
     tb = time.perf_counter()
     for i in range(nb):
         submit(S, pool[i % len(pool)], i)
@@ -660,8 +755,8 @@ def run_serving_workload(args, ckm, torch, dev):
     burst_stats = S.stats()
     S.close()
 
-    # 3. plain per-job loop on the same small jobs (public host-level call)
-    nplain = min(len(pool), args.serve_plain_jobs)
+    # plain per-job loop on the same small jobs (public host-level call)
+    nplain = min(len(pool), plain_jobs)
     tp = time.perf_counter()
     for i in range(nplain):
         _, P, C0, n, d, k = pool[i]
@@ -669,18 +764,39 @@ def run_serving_workload(args, ckm, torch, dev):
     plain_s = (time.perf_counter() - tp) / nplain
 
     cap_rate = nb / burst_s
-    spec = stream(args.serve_rate, args.serve_large_rate, args.serve_seconds, 7)
-    # moderate load: 70 % of the configured small-job rate, same large jobs
-    # (the burst capacity ignores the device time the large jobs take)
-    sustain = stream(0.7 * args.serve_rate, args.serve_large_rate, args.serve_seconds, 8)
-    line = {
+    sampler = ClockSampler(0)
+    sampler.start()
+    spec, ok = stream(rate, large_rate, seconds, 7)
+    clocks = sampler.stop()
+    sustain = None
+    if with_70pct:
+        # moderate load: 70 % of the configured small-job rate, same large jobs
+        # (the burst capacity ignores the device time the large jobs take)
+        sustain, _ = stream(0.7 * rate, large_rate, seconds, 8)
+    check = None
+    if fp64:
+        # served small jobs: centroids against the FP64 means of the labels
+        # they were returned with, masses against the label counts
+        worst, masses_ok, nchk = 0.0, True, 0
+        for r in ok:
+            if r["lane"] != 0 or nchk >= 64:
+                continue
+            _, P, _, n, d, k = pool[r["tag"] % len(pool)]
+            c = fp64_means_check(P, n, d, k, r["labels"], r["centroids"], r["masses"])
+            worst = max(worst, c["max_rel_centroid_err_vs_fp64_means"])
+            masses_ok &= c["masses_equal_label_counts"]
+            nchk += 1
+        check = {"jobs": nchk, "max_rel_centroid_err_vs_fp64_means": worst, "within_1e-5": bool(worst <= 1e-5),
+                 "masses_equal_label_counts": bool(masses_ok)}
+    return {
         "metric": "jobs/s", "value": spec["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": spec["offered_jobs"],
         "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (large jobs: fp16 tensor-core distances, exact FP32 labels)",
         "data": "synthetic (seeded mixtures, pinned host payload pools)",
-        "config": {"workload": "served_stream", "seconds": args.serve_seconds, "small_rate_per_s": args.serve_rate,
-                   "large_rate_per_s": args.serve_large_rate, "small_pool": len(pool), "tolerance": tol,
-                   "max_iterations": cap, "round_iterations": args.serve_round or 4},
+        "config": {"workload": "served_stream", "seconds": seconds, "small_rate_per_s": rate,
+                   "large_rate_per_s": large_rate, "small_pool": len(pool), "tolerance": tol,
+                   "max_iterations": cap, "round_iterations": round_iterations or 4},
+        "latency_ms_small": spec["latency_ms_small"],
         "stream_at_config_rate": spec,
         "stream_at_70pct_config_rate": sustain,
         "burst_capacity_small_jobs_per_s": cap_rate,
@@ -688,21 +804,25 @@ def run_serving_workload(args, ckm, torch, dev):
         "plain_per_job_loop": {"jobs_per_s": 1.0 / plain_s, "jobs": nplain,
                                "call": "ckm_kmeans_run_f32(single_stage, converge) per job"},
         "capacity_vs_plain_loop": cap_rate * plain_s,
+        "fp64_check": check, "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_serving_workload(args, ckm, torch, dev):
+    rec = serving_record(ckm, torch, dev, args.serve_seconds, args.serve_rate, args.serve_large_rate, args.serve_pool,
+                         args.serve_plain_jobs, args.serve_round)
+    print(json.dumps(rec), flush=True)
     return 0
 
 
-def run_tensor_core_workload(args, ckm, torch, dev):
+def tensor_core_record(ckm, torch, dev, n, steps, warmup, simt_compare=True, cpu_baseline=True, fp64=True):
     """Tensor-core labeling with precision recovery: n = 2^24, d = 128,
     k = 1024, a 1024-component mixture (centres ~ N(0, 4 I), sigma
     log-uniform in [0.25, 1], Dirichlet(1) weights), 20 fixed iterations.
     One step = one Lloyd iteration via ckm_tc_fused_f32 (fp16 distance GEMM
     on tcgen05, certified labels, exact FP32 recheck of near-ties, FP64
-    sums)."""
-    n, d, k, iters = 1 << 24, 128, 1024, 20
-    if args.tc_points:
-        n = args.tc_points
+    sums).  Returns the record (a JSON-able dict)."""
+    d, k, iters = 128, 1024, 20
     stream = torch.cuda.current_stream()
     P = torch.empty(n * d, dtype=torch.float32, device=dev)
     ckm.generate_mixture_ex(P, n, d, k, SEED, center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0),
@@ -714,8 +834,8 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     M = torch.empty(k, dtype=torch.int32, device=dev)
     S = ckm.new_scratch(d, k, dev)
     stats = torch.zeros(2, dtype=torch.int32, device=dev)
-    steps = min(args.steps, iters)
-    warm = max(3, min(args.warmup, 5))
+    steps = min(steps, iters)
+    warm = max(3, min(warmup, 5))
     for i in range(warm):
         ckm.tc_fused(P, tcp, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats, stream)
         if i == 0:
@@ -748,23 +868,38 @@ def run_tensor_core_workload(args, ckm, torch, dev):
     flops = 2.0 * n * k * d
     peak, kind = measured_bf16_peak()
     achieved = flops / step_s / 1e12
+    check = None
+    if fp64:
+        # the last step against the FP64 oracle: its labels on a sample of
+        # points from the same input centroids, and its centroids against
+        # the FP64 means of its labels over all points
+        C_in = C[(steps - 1) % 2].cpu().numpy()
+        C_out = C[steps % 2].cpu().numpy()
+        labels = L.cpu().numpy().view(np.uint32)
+        Ph = P.cpu().numpy()
+        rng = np.random.default_rng(5)
+        sample = np.sort(rng.choice(n, size=min(n, 1 << 13), replace=False))
+        Xs = np.ascontiguousarray(Ph.reshape(d, n)[:, sample]).reshape(-1)
+        check = fp64_label_check(Xs, len(sample), d, k, C_in, labels[sample])
+        check.update(fp64_means_check(Ph, n, d, k, labels, C_out, M.cpu().numpy().view(np.uint32)))
+        del Ph
     # the same iteration on the FP32 SIMT path (exact arithmetic everywhere), one step
-    Ls = torch.empty(n, dtype=torch.int32, device=dev)
-    Cs = torch.empty(k * d, dtype=torch.float32, device=dev)
-    Ss = ckm.new_scratch(d, k, dev)
     simt_s = None
-    if not args.no_simt_compare:
+    if simt_compare:
+        Ls = torch.empty(n, dtype=torch.int32, device=dev)
+        Cs = torch.empty(k * d, dtype=torch.float32, device=dev)
+        Ss = ckm.new_scratch(d, k, dev)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ckm.fused(P, C0, Cs, Ls, M, Ss, n, d, k, ckm.MODE_FINALIZE, stream)
         torch.cuda.synchronize()
         simt_s = time.perf_counter() - t0
     cpu = None
-    if not args.no_cpu_baseline:
+    if cpu_baseline:
         n_s = 1 << 12
         Ps = np.ascontiguousarray(P.view(d, n)[:, :n_s].cpu().numpy()).reshape(-1)
         cpu = cpu_baseline_record(Ps, n_s, d, k, 1, "first %d points" % n_s)
-    line = {
+    return {
         "metric": "pts*iter/s", "value": n / step_s, "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
         "warmup": warm, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp16 distances (tcgen05), f32 exact candidates, f64 sums",
@@ -776,13 +911,20 @@ def run_tensor_core_workload(args, ckm, torch, dev):
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_source": kind, "traffic": None,
                      "algorithmic_flops_per_step": flops},
+        "tflops_exact_equivalent": achieved,
         "rechecked_points_per_step": rechecked,
         "resolved_in_kernel_per_step": resolved,
         "overflowed_per_step": overflowed,
+        "fp64_check": check,
         "simt_fp32_step_ms": simt_s * 1e3 if simt_s is not None else None,
         "cpu_baseline": cpu, "gpu_launches": int(gpu_launches), "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_tensor_core_workload(args, ckm, torch, dev):
+    rec = tensor_core_record(ckm, torch, dev, args.tc_points or (1 << 24), args.steps, args.warmup,
+                             simt_compare=not args.no_simt_compare, cpu_baseline=not args.no_cpu_baseline)
+    print(json.dumps(rec), flush=True)
     return 0
 
 
@@ -816,6 +958,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-spatial", action="store_true",
                     help="default workload: time the caller's point order only (no spatial sort, no box pruning)")
+    ap.add_argument("--no-sub-records", action="store_true",
+                    help="default workload: skip the bounded tensor_core / batched / serving records of the line")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the FP64 oracle checks of the line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     workload = args.workload
@@ -926,8 +1071,7 @@ def main():
     bytes_per_point = 4 * d + 4
     achieved = bytes_per_point * n / avg_launch_s / 1e9
     peak, peak_kind = measured_hbm_peak()
-    tpp = profiled_traffic_per_point(workload, "dram_bytes_per_point" if args.no_spatial
-                                     else "dram_bytes_per_point_spatial")
+    tpp = profiled_traffic_per_point("dram_bytes_per_point" if args.no_spatial else "dram_bytes_per_point_spatial")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind,
                 "traffic": (tpp * n) if tpp is not None else None,
@@ -956,10 +1100,19 @@ def main():
                                                    ctypes.byref(info)), "ckm_kmeans_run_f32")
             times.append(time.perf_counter() - t0)
         e2e_t = statistics.mean(times[1:])
+        window_ms = info.total_time_ns / 1e6
         e2e = {"value": n * iters_cfg / e2e_t, "unit": "pts*iter/s",
                "h2d_bytes_per_step": int(info.h2d_bytes), "d2h_bytes_per_step": int(info.d2h_bytes),
                "iterations_per_step": iters_cfg, "ms_per_step": e2e_t * 1e3,
-               "total_time_window_ms": info.total_time_ns / 1e6}
+               "total_time_window_ms": window_ms,
+               "window_roofline_frac": bytes_per_point * n * iters_cfg / (window_ms / 1e3) / 1e9 / peak,
+               "window": "the reference's TotalTime window (kmeans_single_stage.hpp:89-160): the spatial sort "
+                         "and all %d iterations" % iters_cfg}
+        if not args.no_fp64_check and rank == 0:
+            # the call's result against the FP64 oracle: centroids against the
+            # FP64 means of the returned labels, masses against their counts
+            e2e["fp64_check"] = fp64_means_check(hp, n, d, k, hostL.numpy().view(np.uint32), hostC.numpy(),
+                                                 hostM.numpy().view(np.uint32))
         # the link that bounds the copies inside e2e: pinned H2D, 64 MiB chunks
         link_best, _ = ckm.transfer_probe(64 << 20, repeat=16, pinned=True, to_device=True, device=local)
         e2e["h2d_link_gbs"] = link_best
@@ -972,6 +1125,27 @@ def main():
         n_s, it_s = 1 << 22, iters_cfg
         Ps = np.ascontiguousarray(P.view(d, n)[:, :n_s].cpu().numpy()).reshape(-1)
         cpu = cpu_baseline_record(Ps, n_s, d, k, it_s, "first %d points of the workload" % n_s)
+
+    subs = {}
+    if rank == 0 and world == 1 and not args.no_sub_records:
+        # configs 3, 4 and 5 as bounded records of the same line (each in its
+        # own scope, device memory released between them)
+        del P, L, M, S
+        if not args.no_spatial:
+            del Ps, perm
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        fp64 = not args.no_fp64_check
+        for name, fn in (("tensor_core", lambda: tensor_core_record(ckm, torch, dev, 1 << 24, 3, 3, fp64=fp64)),
+                         ("batched", lambda: batched_record(ckm, torch, dev, 4096, 3, 3, fp64=fp64)),
+                         ("serving", lambda: serving_record(ckm, torch, dev, 10.0, 2000.0, 0.5, 512, 100, 0,
+                                                            with_70pct=False, burst_rounds=2, fp64=fp64))):
+            try:
+                subs[name] = fn()
+            except Exception as ex:  # report, keep the headline
+                subs[name] = {"error": "%s: %s" % (type(ex).__name__, ex)}
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
 
     if rank == 0:
         line = {
@@ -988,6 +1162,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(gpu_launches),
             "clocks": clocks, "spatial_order": spatial, "caller_order": unsorted,
         }
+        line.update(subs)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
