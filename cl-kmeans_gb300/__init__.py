@@ -195,16 +195,17 @@ def fused(points, old_centroids, new_centroids, labels, masses, scratch, n, d, k
              scratch.numel(), mode, _stream(stream)), "ckm_fused")
 
 
-def spatial_sort(points, n, d, stream=None):
+def spatial_sort(points, n, d, stream=None, with_perm=True):
     """ckm_spatial_sort_f32: (sorted column-major points, perm) on the points'
-    device; perm[q] is the index in `points` of sorted point q."""
+    device; perm[q] is the index in `points` of sorted point q (None when
+    with_perm is False: the sort then moves no indices)."""
     import torch
     L = lib()
     out = torch.empty_like(points)
-    perm = torch.empty(n, dtype=torch.int32, device=points.device)
+    perm = torch.empty(n, dtype=torch.int32, device=points.device) if with_perm else None
     ws = torch.empty(int(L.ckm_spatial_sort_workspace_bytes(n, d)), dtype=torch.uint8, device=points.device)
-    check(L.ckm_spatial_sort_f32(d, n, _p(points), _p(out), _p(perm), _p(ws), ws.numel(), _stream(stream)),
-          "ckm_spatial_sort_f32")
+    check(L.ckm_spatial_sort_f32(d, n, _p(points), _p(out), _p(perm) if with_perm else None, _p(ws), ws.numel(),
+                                 _stream(stream)), "ckm_spatial_sort_f32")
     return out, perm
 
 

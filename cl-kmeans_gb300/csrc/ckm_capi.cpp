@@ -215,7 +215,7 @@ int ckm_spatial_sort_f32(uint32_t d, uint64_t n, const float* points, float* sor
                          void* workspace, size_t workspace_bytes, ckm_stream_t stream) {
     if (d == 0 || d > 16) return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: num_features must be 1..16");
     if (n > 0xffffffffull) return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: num_points must be < 2^32");
-    if (n > 0 && (!points || !sorted_points || !perm))
+    if (n > 0 && (!points || !sorted_points))
         return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: NULL pointer");
     if (points == sorted_points && n > 0)
         return fail(CKM_ERR_INVALID_ARGUMENT, "spatial sort: sorted_points must not alias points");

@@ -10,17 +10,27 @@
 // of the arithmetic: labels computed on the sorted set go back to the caller's
 // order through the permutation (unpermute).
 //
-//   bbox:      per-feature min / max (order-preserving integer atomics)
-//   per pass (8 key bits, low byte first; the key is recomputed from the
-//   point, and the points and their original indices travel with it):
-//   upsweep:   per chunk (CHUNK consecutive items), the count of each digit
-//   scan:      exclusive prefix of the counts in digit-major order: where each
-//              (digit, chunk) run starts in the output
-//   downsweep: each CTA ranks its chunk's items by digit, stably, in shared
-//              memory (rounds of 256 items, warp match + per-warp counts), and
-//              writes each digit's run contiguously (coalesced), gathering
-//              the points from the chunk it has just read
+// The pipeline moves each point a minimal number of times (at n = 2^28,
+// d = 4: two reads and two writes of the 4 GiB of points, plus 2-byte keys):
+//   bbox:     per-feature min / max over a strided sample of 2^20 points
+//             (points outside the sample's range fall in the edge cells);
+//   keys:     one pass over the points: the 16-bit key of every point into a
+//             padded key array, and per chunk of CH consecutive points the
+//             histogram of the key's low byte;
+//   scan:     exclusive prefix of the chunk histograms in digit-major order
+//             (where each (digit, chunk) run starts in the output), stored
+//             chunk-major so a chunk reads its 256 offsets in one 1 KiB row;
+//   scatter:  per chunk, the keys and then the points (and indices) are
+//             staged in shared memory by cp.async; while the points are in
+//             flight the chunk's items are ranked stably within their digits
+//             (warps own contiguous runs of items; warp match + per-warp
+//             counts; one pass); then every digit's run is written out
+//             contiguously (coalesced), reading the staged points;
+//   pass 2:   the histogram of the high byte over the pass-1 keys (2 bytes a
+//             point), the scan, and the same scatter on the high byte.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "ckm_device.cuh"
 #include "ckm_internal.h"
@@ -28,7 +38,11 @@
 namespace ckm {
 namespace {
 
-constexpr int SB = 256;
+constexpr int SB = 512;                      // threads per CTA: key, histogram and scatter kernels
+constexpr uint32_t RADIX = 256;
+constexpr uint32_t BBOX_SAMPLES = 1u << 20;  // points sampled for the bounding box
+constexpr uint32_t SCAN_ROWS = 256;          // chunks per block of the offset scan
+constexpr uint32_t SCAN_BATCH = 16;          // independent rows loaded together in the scan
 
 __device__ __forceinline__ uint32_t ord_of(float x) {
     const uint32_t b = __float_as_uint(x);
@@ -38,48 +52,98 @@ __device__ __forceinline__ float float_of(uint32_t u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-// Workspace: [0, 16) min (ordered), [16, 32) max (ordered), the counts /
-// offsets [RADIX * chunks], the scan's block sums, then the intermediate
-// points [d * n] and indices [n] between the two passes.
-constexpr uint32_t RADIX = 256;
-constexpr uint32_t SCAN_PER_BLOCK = 4096;
+// Points per chunk: a chunk's staged points are 64 KiB for every d (4096
+// points for d <= 4).  512-thread CTAs, two per SM, rank and write a chunk
+// each (a 256-thread shape on half the chunk measured 20 % slower).
+__host__ __device__ constexpr uint32_t chunk_of(uint32_t d) { return 4096u / (d <= 4 ? 1u : (d <= 8 ? 2u : 4u)); }
+uint32_t chunk_items(uint32_t d) { return chunk_of(d); }
+uint64_t num_chunks(uint64_t n, uint32_t d) { return (n + chunk_items(d) - 1) / chunk_items(d); }
+uint64_t scan_blocks_of(uint64_t chunks) { return (chunks + SCAN_ROWS - 1) / SCAN_ROWS; }
+size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// Workspace: [0, 64) min (ordered), [64, 128) max (ordered); the chunk
+// offsets [chunks][RADIX]; the scan's block partials [blocks + 1][RADIX]; two
+// padded key arrays [chunks * CH]; the points [d * n] and indices [n] between
+// the two passes.
 struct SortWs {
     uint32_t* lo;
     uint32_t* hi;
     uint32_t* counts;
-    uint32_t* block_sums;
+    uint32_t* partial;
+    uint16_t* keys0;
+    uint16_t* keys1;
     float* tmp_points;
     uint32_t* tmp_idx;
 };
 
-// Items per chunk: the chunk is re-read (gathered) from L2 when written out, so
-// it stays a 64 KiB window of points.
-uint32_t chunk_items(uint32_t d) { return d <= 4 ? 4096u : (d <= 8 ? 2048u : 1024u); }
-
-uint64_t num_chunks(uint64_t n, uint32_t d) { return (n + chunk_items(d) - 1) / chunk_items(d); }
-
-size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
-
-uint64_t scan_blocks_of(uint64_t n, uint32_t d) {
-    return ((uint64_t)RADIX * num_chunks(n, d) + SCAN_PER_BLOCK - 1) / SCAN_PER_BLOCK;
+struct WsSizes {
+    size_t counts, partial, keys, pts, idx;
+};
+WsSizes ws_sizes(uint64_t n, uint32_t d) {
+    WsSizes z;
+    const uint64_t ch = chunk_of(d), chunks = (n + ch - 1) / ch;
+    z.counts = a256((size_t)RADIX * chunks * 4);
+    z.partial = a256((size_t)RADIX * (scan_blocks_of(chunks) + 1) * 4);
+    z.keys = a256((size_t)chunks * ch * 2);
+    z.pts = a256((size_t)n * d * 4);
+    z.idx = a256((size_t)n * 4);
+    return z;
 }
 
 SortWs sort_ws(void* ws, uint64_t n, uint32_t d) {
     unsigned char* w = static_cast<unsigned char*>(ws);
-    const size_t counts = a256((size_t)RADIX * num_chunks(n, d) * 4);
-    const size_t sums = a256((size_t)scan_blocks_of(n, d) * 4);
+    const WsSizes z = ws_sizes(n, d);
     SortWs r;
+    size_t off = 256;
     r.lo = reinterpret_cast<uint32_t*>(w);
     r.hi = r.lo + 16;
-    r.counts = reinterpret_cast<uint32_t*>(w + 256);
-    r.block_sums = reinterpret_cast<uint32_t*>(w + 256 + counts);
-    r.tmp_points = reinterpret_cast<float*>(w + 256 + counts + sums);
-    r.tmp_idx = reinterpret_cast<uint32_t*>(w + 256 + counts + sums + a256((size_t)n * d * 4));
+    r.counts = reinterpret_cast<uint32_t*>(w + off);
+    off += z.counts;
+    r.partial = reinterpret_cast<uint32_t*>(w + off);
+    off += z.partial;
+    r.keys0 = reinterpret_cast<uint16_t*>(w + off);
+    off += z.keys;
+    r.keys1 = reinterpret_cast<uint16_t*>(w + off);
+    off += z.keys;
+    r.tmp_points = reinterpret_cast<float*>(w + off);
+    off += z.pts;
+    r.tmp_idx = reinterpret_cast<uint32_t*>(w + off);
     return r;
 }
 
-__global__ void __launch_bounds__(SB) bbox_kernel(const float* __restrict__ P, uint64_t n, uint32_t d, SortWs ws) {
+// --- cp.async (per-thread asynchronous global -> shared copies) ------------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Copies count 32-bit words src[0, count) to dst (shared) with 16-byte copies
+// where both sides allow it (vec: src 16-byte aligned), 4-byte ones for the
+// rest; every thread of the CTA takes part.
+template <int BT>
+__device__ __forceinline__ void stage_words(uint32_t* dst, const uint32_t* src, uint32_t count, bool vec) {
+    uint32_t done = 0;
+    if (vec) {
+        const uint32_t nv = count / 4;
+        for (uint32_t i = threadIdx.x; i < nv; i += BT) cp_async16(dst + 4 * i, src + 4 * i);
+        done = nv * 4;
+    }
+    for (uint32_t i = done + threadIdx.x; i < count; i += BT) cp_async4(dst + i, src + i);
+}
+
+// --- bounding box from a strided sample ------------------------------------
+__global__ void __launch_bounds__(256) bbox_sample_kernel(const float* __restrict__ P, uint64_t n, uint32_t d,
+                                                          uint64_t stride, uint32_t samples, uint32_t* lo_out,
+                                                          uint32_t* hi_out) {
     __shared__ uint32_t s_lo[16], s_hi[16];
     if (threadIdx.x < 16) {
         s_lo[threadIdx.x] = 0xffffffffu;
@@ -88,8 +152,8 @@ __global__ void __launch_bounds__(SB) bbox_kernel(const float* __restrict__ P, u
     __syncthreads();
     for (uint32_t f = 0; f < d; ++f) {
         float lo = INFINITY, hi = -INFINITY;
-        for (uint64_t p = (uint64_t)blockIdx.x * SB + threadIdx.x; p < n; p += (uint64_t)gridDim.x * SB) {
-            const float v = __ldg(P + (size_t)f * n + p);
+        for (uint32_t i = blockIdx.x * 256u + threadIdx.x; i < samples; i += gridDim.x * 256u) {
+            const float v = __ldg(P + (size_t)f * n + (uint64_t)i * stride);
             lo = fminf(lo, v);  // NaN ignored
             hi = fmaxf(hi, v);
         }
@@ -102,202 +166,316 @@ __global__ void __launch_bounds__(SB) bbox_kernel(const float* __restrict__ P, u
     }
     __syncthreads();
     if (threadIdx.x < d) {
-        atomicMin(&ws.lo[threadIdx.x], s_lo[threadIdx.x]);
-        atomicMax(&ws.hi[threadIdx.x], s_hi[threadIdx.x]);
+        atomicMin(&lo_out[threadIdx.x], s_lo[threadIdx.x]);
+        atomicMax(&hi_out[threadIdx.x], s_hi[threadIdx.x]);
     }
 }
 
-// Z-order key of point p (b bits per feature, d * b <= 16).
-__device__ __forceinline__ uint32_t point_key(const float* __restrict__ P, uint64_t n, uint64_t p, uint32_t d,
-                                              uint32_t b, const float* lo, const float* scale) {
-    const uint32_t top = (1u << b) - 1u;
+// Bin origin and scale of each feature (threads < d; into shared memory).
+__device__ __forceinline__ void load_range(const uint32_t* lo_w, const uint32_t* hi_w, uint32_t d, uint32_t b,
+                                           float* s_lo, float* s_scale) {
+    if (threadIdx.x < d) {
+        const uint32_t f = threadIdx.x;
+        const float l = float_of(lo_w[f]), h = float_of(hi_w[f]);
+        const float w = h - l;
+        s_scale[f] = (w > 0.0f && w < INFINITY) ? (float)(1u << b) / w : 0.0f;
+        s_lo[f] = (l > -INFINITY && l < INFINITY) ? l : 0.0f;
+    }
+}
+
+// Z-order key of one point from its D coordinates (B = 16 / D bits per
+// feature, B = 1 for D > 8): feature f's bin q_f contributes bit i at
+// position i * D + f.
+// Bits of q (B of them) moved to every D-th position, bit i to i * D.
+template <int D>
+__device__ __forceinline__ uint32_t spread_bits(uint32_t q) {
+    if constexpr (D == 4) {  // 4 bits -> 0, 4, 8, 12
+        q = (q | (q << 6)) & 0x0303u;
+        return (q | (q << 3)) & 0x1111u;
+    } else if constexpr (D == 2) {  // 8 bits -> 0, 2, ..., 14
+        q = (q | (q << 4)) & 0x0f0fu;
+        q = (q | (q << 2)) & 0x3333u;
+        return (q | (q << 1)) & 0x5555u;
+    } else if constexpr (D == 8) {  // 2 bits -> 0, 8
+        return (q & 1u) | ((q & 2u) << 7);
+    } else {
+        constexpr uint32_t B = D >= 16 ? 1u : 16u / D;
+        uint32_t r = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < B; ++i) r |= ((q >> i) & 1u) << (i * D);
+        return r;
+    }
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t z_key(const float (&v)[D], const float* s_lo, const float* s_scale) {
+    constexpr uint32_t B = D >= 16 ? 1u : 16u / D;
+    constexpr float TOP = (float)((1u << B) - 1u);
     uint32_t key = 0;
-    for (uint32_t f = 0; f < d; ++f) {
-        const float v = (__ldg(P + (size_t)f * n + p) - lo[f]) * scale[f];
+#pragma unroll
+    for (int f = 0; f < D; ++f) {
         // NaN and values below the range go to bin 0, above it to the top bin
-        const uint32_t q = v >= (float)top ? top : (v >= 1.0f ? (uint32_t)v : 0u);
-        for (uint32_t i = 0; i < b; ++i) key |= ((q >> i) & 1u) << (i * d + f);
+        const float x = fminf(fmaxf((v[f] - s_lo[f]) * s_scale[f], 0.0f), TOP);
+        key |= spread_bits<D>((uint32_t)x) << f;
     }
     return key;
 }
 
-__device__ __forceinline__ void load_range(const SortWs& ws, uint32_t d, uint32_t b, float* lo, float* scale) {
-    for (uint32_t f = 0; f < d; ++f) {
-        const float l = float_of(ws.lo[f]), h = float_of(ws.hi[f]);
-        lo[f] = l;
-        const float w = h - l;
-        scale[f] = (w > 0.0f && w < INFINITY) ? (float)(1u << b) / w : 0.0f;
-        if (!(l > -INFINITY && l < INFINITY)) lo[f] = 0.0f;
+// Warp-aggregated count of one digit per lane into a shared histogram.
+__device__ __forceinline__ void count_digit(uint32_t* s_hist, uint32_t dg, bool ok) {
+    const uint32_t active = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+        const uint32_t peers = __match_any_sync(active, dg);
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_hist[dg], (uint32_t)__popc(peers));
     }
 }
 
-// Digit (8 bits at `shift`) of item i of a pass's input.
-__device__ __forceinline__ uint32_t item_digit(const float* __restrict__ P, uint64_t n, uint64_t i, uint32_t d,
-                                               uint32_t b, const float* lo, const float* scale, uint32_t shift) {
-    return (point_key(P, n, i, d, b, lo, scale) >> shift) & (RADIX - 1u);
-}
-
-// Digit histogram of one chunk into s_hist (warp-aggregated shared atomics);
-// every thread of the CTA calls it.
-__device__ __forceinline__ void chunk_histogram(const float* __restrict__ P, uint64_t n, uint32_t d, uint32_t b,
-                                                const float* lo, const float* scale, uint32_t shift, uint64_t c0,
-                                                uint32_t chunk, uint32_t* s_hist) {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t j = threadIdx.x; j < RADIX; j += SB) s_hist[j] = 0u;
-    __syncthreads();
-    for (uint32_t r = 0; r < chunk; r += SB) {
-        const uint64_t i = c0 + r + threadIdx.x;
-        const bool ok = i < n;
-        const uint32_t active = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            const uint32_t dg = item_digit(P, n, i, d, b, lo, scale, shift);
-            const uint32_t peers = __match_any_sync(active, dg);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_hist[dg], (uint32_t)__popc(peers));
-        }
-    }
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(SB) upsweep_kernel(const float* __restrict__ P, uint64_t n, uint32_t d, uint32_t b,
-                                                     SortWs ws, uint32_t shift, uint32_t chunk, uint64_t chunks) {
+// keys[c0 + j] for the chunk's points (0 for the padding past n) and the
+// chunk's histogram of the low key byte, counts[chunk][digit].  Every
+// coordinate of the thread's IPT points is loaded before any key is formed,
+// so the loads are in flight together; with 16-byte aligned rows (vec) a
+// thread's points are consecutive and each feature row is read in 16-byte
+// loads.
+template <int D, uint32_t CH, int BT>
+__global__ void __launch_bounds__(BT) key_kernel(const float* __restrict__ P, uint64_t n,
+                                                 const uint32_t* __restrict__ lo_w, const uint32_t* __restrict__ hi_w,
+                                                 int vec, uint16_t* __restrict__ keys, uint32_t* __restrict__ counts) {
+    constexpr uint32_t IPT = CH / BT;
+    static_assert(IPT % 4 == 0 || IPT == 2, "4-point groups per thread");
+    constexpr uint32_t B = D >= 16 ? 1u : 16u / D;
     __shared__ uint32_t s_hist[RADIX];
-    float lo[16], scale[16];
-    load_range(ws, d, b, lo, scale);
-    const uint64_t c = blockIdx.x;
-    chunk_histogram(P, n, d, b, lo, scale, shift, c * chunk, chunk, s_hist);
-    for (uint32_t j = threadIdx.x; j < RADIX; j += SB) ws.counts[(uint64_t)j * chunks + c] = s_hist[j];
-}
-
-// Exclusive scan of counts[0, m) in place: block sums, then their scan, then
-// each block's prefix.
-__global__ void __launch_bounds__(SB) scan_sums_kernel(const uint32_t* __restrict__ v, uint64_t m, uint32_t* sums) {
-    __shared__ uint32_t s_w[SB / 32];
-    const uint64_t b0 = (uint64_t)blockIdx.x * SCAN_PER_BLOCK;
-    uint32_t t = 0;
-    for (uint32_t j = threadIdx.x; j < SCAN_PER_BLOCK; j += SB)
-        if (b0 + j < m) t += v[b0 + j];
-    t = __reduce_add_sync(0xffffffffu, t);
-    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = t;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t s = 0;
-        for (int w = 0; w < SB / 32; ++w) s += s_w[w];
-        sums[blockIdx.x] = s;
-    }
-}
-
-__global__ void __launch_bounds__(1024) scan_block_sums_kernel(uint32_t* sums, uint32_t nb) {
-    // exclusive scan of nb values: each thread a run of ceil(nb / 1024)
-    __shared__ uint32_t s_part[1024];
-    const uint32_t t = threadIdx.x;
-    const uint32_t per = (nb + 1023u) / 1024u;
-    const uint32_t j0 = t * per;
-    uint32_t tot = 0;
-    for (uint32_t i = 0; i < per; ++i)
-        if (j0 + i < nb) tot += sums[j0 + i];
-    s_part[t] = tot;
-    __syncthreads();
-    for (uint32_t o = 1; o < 1024; o <<= 1) {
-        const uint32_t x = t >= o ? s_part[t - o] : 0u;
-        __syncthreads();
-        s_part[t] += x;
-        __syncthreads();
-    }
-    uint32_t run = s_part[t] - tot;
-    for (uint32_t i = 0; i < per; ++i)
-        if (j0 + i < nb) {
-            const uint32_t v = sums[j0 + i];
-            sums[j0 + i] = run;
-            run += v;
+    __shared__ float s_lo[16], s_scale[16];
+    load_range(lo_w, hi_w, D, B, s_lo, s_scale);
+    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) s_hist[j] = 0u;
+    const uint64_t c0 = (uint64_t)blockIdx.x * CH;
+    const bool seq = vec && IPT % 4 == 0;  // thread's points consecutive
+    float v[IPT][D];
+    if (seq && c0 + CH <= n) {
+        const uint64_t p0 = c0 + (uint64_t)IPT * threadIdx.x;
+#pragma unroll
+        for (int f = 0; f < D; ++f)
+#pragma unroll
+            for (uint32_t r = 0; r < IPT; r += 4) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(P + (size_t)f * n + p0 + r));
+                v[r][f] = q.x;
+                v[r + 1][f] = q.y;
+                v[r + 2][f] = q.z;
+                v[r + 3][f] = q.w;
+            }
+    } else {
+#pragma unroll
+        for (uint32_t r = 0; r < IPT; ++r) {
+            const uint64_t p = seq ? c0 + (uint64_t)IPT * threadIdx.x + r : c0 + r * BT + threadIdx.x;
+#pragma unroll
+            for (int f = 0; f < D; ++f) v[r][f] = p < n ? __ldg(P + (size_t)f * n + p) : 0.0f;
         }
-}
-
-__global__ void __launch_bounds__(SB) scan_apply_kernel(uint32_t* v, uint64_t m, const uint32_t* __restrict__ sums) {
-    // per block: 16 consecutive values per thread, a block scan of the
-    // thread totals, plus the block's offset
-    __shared__ uint32_t s_part[SB];
-    const uint64_t b0 = (uint64_t)blockIdx.x * SCAN_PER_BLOCK;
-    const uint32_t per = SCAN_PER_BLOCK / SB;
-    const uint64_t j0 = b0 + (uint64_t)threadIdx.x * per;
-    uint32_t x[SCAN_PER_BLOCK / SB], tot = 0;
-    for (uint32_t i = 0; i < per; ++i) {
-        x[i] = j0 + i < m ? v[j0 + i] : 0u;
-        tot += x[i];
     }
-    s_part[threadIdx.x] = tot;
     __syncthreads();
-    for (uint32_t o = 1; o < SB; o <<= 1) {
-        const uint32_t y = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        s_part[threadIdx.x] += y;
-        __syncthreads();
+#pragma unroll
+    for (uint32_t r = 0; r < IPT; ++r) {
+        const uint64_t p = seq ? c0 + (uint64_t)IPT * threadIdx.x + r : c0 + r * BT + threadIdx.x;
+        const uint32_t key = p < n ? z_key<D>(v[r], s_lo, s_scale) : 0u;
+        keys[p] = (uint16_t)key;
+        count_digit(s_hist, key & (RADIX - 1u), p < n);
     }
-    uint32_t run = sums[blockIdx.x] + s_part[threadIdx.x] - tot;
-    for (uint32_t i = 0; i < per; ++i) {
-        if (j0 + i < m) v[j0 + i] = run;
-        run += x[i];
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) counts[(uint64_t)blockIdx.x * RADIX + j] = s_hist[j];
+}
+
+template <int D>
+void launch_key_kernel(uint64_t chunks, const float* P, uint64_t n, const uint32_t* lo, const uint32_t* hi, int vec,
+                       uint16_t* keys, uint32_t* counts, cudaStream_t s) {
+    key_kernel<D, chunk_of(D), SB><<<(unsigned)chunks, SB, 0, s>>>(P, n, lo, hi, vec, keys, counts);
+}
+
+void launch_keys(uint32_t d, uint64_t chunks, const float* P, uint64_t n, const uint32_t* lo, const uint32_t* hi,
+                 int vec, uint16_t* keys, uint32_t* counts, cudaStream_t s) {
+    switch (d) {
+#define CKM_KEY_CASE(DD) \
+    case DD: launch_key_kernel<DD>(chunks, P, n, lo, hi, vec, keys, counts, s); break;
+        CKM_KEY_CASE(1) CKM_KEY_CASE(2) CKM_KEY_CASE(3) CKM_KEY_CASE(4) CKM_KEY_CASE(5) CKM_KEY_CASE(6)
+        CKM_KEY_CASE(7) CKM_KEY_CASE(8) CKM_KEY_CASE(9) CKM_KEY_CASE(10) CKM_KEY_CASE(11) CKM_KEY_CASE(12)
+        CKM_KEY_CASE(13) CKM_KEY_CASE(14) CKM_KEY_CASE(15)
+#undef CKM_KEY_CASE
+        default: launch_key_kernel<16>(chunks, P, n, lo, hi, vec, keys, counts, s); break;
     }
 }
 
-// One pass's scatter for one chunk:
-//   1. the chunk's items are read once (coalesced); their digits go to shared
-//      memory and into the chunk's histogram;
-//   2. the items are ranked stably within their digits in rounds of SB (item
-//      order = round, then thread; warp match + per-warp counts), entirely in
-//      shared memory: s_src[pos] = the chunk-local index of the item at
-//      position pos of the chunk sorted by digit;
-//   3. the sorted chunk is written out digit run by digit run (consecutive
-//      output positions, coalesced), gathering the point values from the
-//      chunk just read (an L2-resident window).
-__global__ void __launch_bounds__(SB) downsweep_kernel(const float* __restrict__ P, const uint32_t* __restrict__ idx_in,
-                                                       uint64_t n, uint32_t d, uint32_t b, SortWs ws, uint32_t shift,
-                                                       uint32_t chunk, uint64_t chunks, float* __restrict__ P_out,
-                                                       uint32_t* __restrict__ idx_out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint16_t* s_src = reinterpret_cast<uint16_t*>(smem);                 // [chunk]
-    unsigned char* s_din = reinterpret_cast<unsigned char*>(s_src + chunk);  // digit of local item j
-    unsigned char* s_dig = s_din + chunk;                                 // digit at sorted position
-    constexpr uint32_t NW = SB / 32;
-    // per warp and digit: the warp's count, then the absolute position of its
-    // next item of that digit
-    __shared__ uint32_t s_off[RADIX], s_wh[NW][RADIX], s_ws[NW];
-    float lo[16], scale[16];
-    load_range(ws, d, b, lo, scale);
-    const uint64_t c = blockIdx.x;
-    const uint64_t c0 = c * chunk;
-    const uint32_t valid = (uint32_t)min((uint64_t)chunk, n - c0);
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    // each warp owns a contiguous run of the chunk's items (chunk is a
-    // multiple of SB), so only warp-level synchronisation is needed while
-    // digits are counted and positions handed out; the warps' runs in order
-    // keep the sort stable
-    const uint32_t per = chunk / NW, w0 = warp * per;
+// counts[chunk][digit] of the key byte at `shift` over a padded key array.
+template <uint32_t CH, int BT>
+__global__ void __launch_bounds__(BT) hist_kernel(const uint16_t* __restrict__ keys, uint64_t n, uint32_t shift,
+                                                  uint32_t* __restrict__ counts) {
+    constexpr uint32_t IPT = CH / BT;  // 8, 4 or 2 consecutive keys per thread: one 16, 8 or 4-byte load
+    __shared__ uint32_t s_hist[RADIX];
+    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) s_hist[j] = 0u;
+    __syncthreads();
+    const uint64_t p0 = (uint64_t)blockIdx.x * CH + threadIdx.x * IPT;
+    uint16_t k[IPT];
+    if constexpr (IPT == 8) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(keys + p0));
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            k[2 * i] = (uint16_t)(w[i] & 0xffffu);
+            k[2 * i + 1] = (uint16_t)(w[i] >> 16);
+        }
+    } else if constexpr (IPT == 4) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(keys + p0));
+        k[0] = (uint16_t)(v.x & 0xffffu);
+        k[1] = (uint16_t)(v.x >> 16);
+        k[2] = (uint16_t)(v.y & 0xffffu);
+        k[3] = (uint16_t)(v.y >> 16);
+    } else {
+        static_assert(IPT == 2, "2, 4 or 8 keys per thread");
+        const uint32_t v = __ldg(reinterpret_cast<const unsigned int*>(keys + p0));
+        k[0] = (uint16_t)(v & 0xffffu);
+        k[1] = (uint16_t)(v >> 16);
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < IPT; ++r) count_digit(s_hist, ((uint32_t)k[r] >> shift) & (RADIX - 1u), p0 + r < n);
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) counts[(uint64_t)blockIdx.x * RADIX + j] = s_hist[j];
+}
 
-    // 1. digits and per-warp histograms
-    for (uint32_t t = lane; t < RADIX; t += 32) s_wh[warp][t] = 0u;
-    __syncwarp();
-    for (uint32_t r = 0; r < per; r += 32) {
-        const uint32_t j = w0 + r + lane;
+// --- exclusive scan of counts[chunk][digit] in digit-major order ----------
+// partial[blk][digit] = the total of the digit over the block's SCAN_ROWS chunks
+__global__ void __launch_bounds__(RADIX) scan_partial_kernel(const uint32_t* __restrict__ counts, uint64_t rows,
+                                                             uint32_t* __restrict__ partial) {
+    const uint64_t r0 = (uint64_t)blockIdx.x * SCAN_ROWS;
+    const uint64_t r1 = min(rows, r0 + SCAN_ROWS);
+    uint32_t t = 0;
+    for (uint64_t r = r0; r < r1; r += SCAN_BATCH) {
+        uint32_t v[SCAN_BATCH];
+#pragma unroll
+        for (uint32_t i = 0; i < SCAN_BATCH; ++i) v[i] = r + i < r1 ? counts[(r + i) * RADIX + threadIdx.x] : 0u;
+#pragma unroll
+        for (uint32_t i = 0; i < SCAN_BATCH; ++i) t += v[i];
+    }
+    partial[(uint64_t)blockIdx.x * RADIX + threadIdx.x] = t;
+}
+
+// One CTA: partial[blk][digit] becomes the exclusive prefix of the digit
+// over the blocks, and row nblk the start of each digit's output range (the
+// totals of the smaller digits).
+__global__ void __launch_bounds__(RADIX) scan_top_kernel(uint32_t* __restrict__ partial, uint32_t nblk) {
+    __shared__ uint32_t s_w[RADIX / 32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    uint32_t run = 0;
+    for (uint32_t b0 = 0; b0 < nblk; b0 += SCAN_BATCH) {
+        uint32_t v[SCAN_BATCH];
+#pragma unroll
+        for (uint32_t i = 0; i < SCAN_BATCH; ++i) v[i] = b0 + i < nblk ? partial[(uint64_t)(b0 + i) * RADIX + t] : 0u;
+#pragma unroll
+        for (uint32_t i = 0; i < SCAN_BATCH; ++i)
+            if (b0 + i < nblk) {
+                partial[(uint64_t)(b0 + i) * RADIX + t] = run;
+                run += v[i];
+            }
+    }
+    uint32_t incl = run;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    uint32_t base = incl - run;
+    for (uint32_t w = 0; w < warp; ++w) base += s_w[w];
+    partial[(uint64_t)nblk * RADIX + t] = base;
+}
+
+// counts[chunk][digit] = where the chunk's run of the digit starts
+__global__ void __launch_bounds__(RADIX) scan_apply_kernel(uint32_t* __restrict__ counts, uint64_t rows,
+                                                           const uint32_t* __restrict__ partial, uint32_t nblk) {
+    const uint64_t r0 = (uint64_t)blockIdx.x * SCAN_ROWS;
+    const uint64_t r1 = min(rows, r0 + SCAN_ROWS);
+    uint32_t run = partial[(uint64_t)blockIdx.x * RADIX + threadIdx.x] + partial[(uint64_t)nblk * RADIX + threadIdx.x];
+    for (uint64_t r = r0; r < r1; r += SCAN_BATCH) {
+        uint32_t v[SCAN_BATCH];
+#pragma unroll
+        for (uint32_t i = 0; i < SCAN_BATCH; ++i) v[i] = r + i < r1 ? counts[(r + i) * RADIX + threadIdx.x] : 0u;
+#pragma unroll
+        for (uint32_t i = 0; i < SCAN_BATCH; ++i)
+            if (r + i < r1) {
+                counts[(r + i) * RADIX + threadIdx.x] = run;
+                run += v[i];
+            }
+    }
+}
+
+// --- one scatter pass ------------------------------------------------------
+// Dynamic shared memory: s_pts [d][CH] f32, s_key [CH] u16, s_src [CH] u16,
+// s_idx [CH] u32 (only with idx_in).
+size_t scatter_smem(uint32_t d, bool with_idx) {
+    const size_t ch = chunk_items(d);
+    return ch * d * 4 + ch * 2 + ch * 2 + (with_idx ? ch * 4 : 0);
+}
+
+template <uint32_t CH, int BT>
+__global__ void __launch_bounds__(BT, 1024 / BT)
+    scatter_kernel(const float* __restrict__ P, const uint32_t* __restrict__ idx_in, const uint16_t* __restrict__ keys,
+                   uint64_t n, uint32_t d, uint32_t shift, const uint32_t* __restrict__ offsets, int vec,
+                   float* __restrict__ P_out, uint16_t* __restrict__ keys_out, uint32_t* __restrict__ idx_out) {
+    constexpr uint32_t NW = BT / 32;
+    constexpr uint32_t IPW = CH / NW;        // items of a warp (a contiguous run)
+    constexpr uint32_t ROUNDS = IPW / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* s_pts = reinterpret_cast<float*>(smem);
+    uint16_t* s_key = reinterpret_cast<uint16_t*>(s_pts + (size_t)d * CH);
+    uint16_t* s_src = s_key + CH;
+    uint32_t* s_idx = reinterpret_cast<uint32_t*>(s_src + CH);
+    // per warp and digit: the count of the digit in the warp's earlier
+    // rounds, then (after the scan) the digit's items in earlier warps
+    __shared__ uint16_t s_wh[NW][RADIX];
+    __shared__ uint32_t s_off[RADIX], s_base[RADIX], s_wsum[RADIX / 32];
+
+    const uint64_t c0 = (uint64_t)blockIdx.x * CH;
+    const uint32_t valid = (uint32_t)min((uint64_t)CH, n - c0);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+
+    // 1. stage the keys (group 0), then the points and indices (group 1)
+    stage_words<BT>(reinterpret_cast<uint32_t*>(s_key), reinterpret_cast<const uint32_t*>(keys + c0), CH / 2, true);
+    cp_async_commit();
+    for (uint32_t f = 0; f < d; ++f)
+        stage_words<BT>(reinterpret_cast<uint32_t*>(s_pts + (size_t)f * CH),
+                        reinterpret_cast<const uint32_t*>(P + (size_t)f * n + c0), valid, vec != 0);
+    if (idx_in) stage_words<BT>(s_idx, idx_in + c0, valid, true);
+    cp_async_commit();
+    for (uint32_t t = lane; t < RADIX; t += 32) s_wh[warp][t] = 0;
+    cp_async_wait<1>();
+    __syncthreads();
+
+    // 2. stable ranks within (warp, digit): warp w owns items
+    //    [w * IPW, (w + 1) * IPW), in rounds of 32 consecutive items
+    uint32_t dig[ROUNDS], rank[ROUNDS];
+#pragma unroll
+    for (uint32_t r = 0; r < ROUNDS; ++r) {
+        const uint32_t j = warp * IPW + r * 32 + lane;
         const bool ok = j < valid;
         const uint32_t active = __ballot_sync(0xffffffffu, ok);
+        dig[r] = 0;
+        rank[r] = 0;
         if (ok) {
-            const uint32_t dg = item_digit(P, n, c0 + j, d, b, lo, scale, shift);
-            s_din[j] = (unsigned char)dg;
+            const uint32_t dg = ((uint32_t)s_key[j] >> shift) & (RADIX - 1u);
             const uint32_t peers = __match_any_sync(active, dg);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wh[warp][dg] += (uint32_t)__popc(peers);
+            dig[r] = dg;
+            rank[r] = (uint32_t)s_wh[warp][dg] + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            __syncwarp(active);  // every lane has read the count before the leader moves it
+            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wh[warp][dg] += (uint16_t)__popc(peers);
         }
         __syncwarp();
     }
     __syncthreads();
 
-    // 2. thread t = digit t (SB == RADIX): the counts of the warps before each
-    // warp, the digit's total, and the exclusive scan of the totals
-    {
+    // 3. thread t < RADIX = digit t: the counts of the warps before each
+    //    warp, the digit's chunk-local start, and its place in the output
+    if (threadIdx.x < RADIX) {
         const uint32_t t = threadIdx.x;
         uint32_t tot = 0;
         for (uint32_t w = 0; w < NW; ++w) {
             const uint32_t v = s_wh[w][t];
-            s_wh[w][t] = tot;
+            s_wh[w][t] = (uint16_t)tot;
             tot += v;
         }
         uint32_t incl = tot;
@@ -306,68 +484,110 @@ __global__ void __launch_bounds__(SB) downsweep_kernel(const float* __restrict__
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += y;
         }
-        if (lane == 31) s_ws[warp] = incl;
-        __syncthreads();
-        uint32_t base = 0;
-        for (uint32_t w = 0; w < warp; ++w) base += s_ws[w];
-        const uint32_t excl = base + incl - tot;
+        if (lane == 31) s_wsum[warp] = incl;
+        asm volatile("bar.sync 1, %0;" ::"r"(RADIX));  // the digit threads only
+        uint32_t excl = incl - tot;
+        for (uint32_t w = 0; w < warp; ++w) excl += s_wsum[w];
         s_off[t] = excl;
-        for (uint32_t w = 0; w < NW; ++w) s_wh[w][t] += excl;
+        s_base[t] = offsets[(uint64_t)blockIdx.x * RADIX + t] - excl;  // mod 2^32: base + q < 2^32
     }
     __syncthreads();
 
-    // 3. stable positions: each warp hands out positions to its items in order
-    for (uint32_t r = 0; r < per; r += 32) {
-        const uint32_t j = w0 + r + lane;
-        const bool ok = j < valid;
-        const uint32_t active = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            const uint32_t dg = s_din[j];
-            const uint32_t peers = __match_any_sync(active, dg);
-            const uint32_t pos = s_wh[warp][dg] + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-            s_src[pos] = (uint16_t)j;
-            s_dig[pos] = (unsigned char)dg;
-            __syncwarp(active);  // every lane has read its base before the leader moves it
-            if (lane == (uint32_t)(__ffs(peers) - 1)) s_wh[warp][dg] += (uint32_t)__popc(peers);
-        }
-        __syncwarp();
+    // 4. sorted chunk position of each item
+#pragma unroll
+    for (uint32_t r = 0; r < ROUNDS; ++r) {
+        const uint32_t j = warp * IPW + r * 32 + lane;
+        if (j < valid) s_src[s_off[dig[r]] + s_wh[warp][dig[r]] + rank[r]] = (uint16_t)j;
     }
+    cp_async_wait<0>();
     __syncthreads();
 
-    // 3. write out
-    for (uint32_t q = threadIdx.x; q < valid; q += SB) {
-        const uint32_t dg = s_dig[q];
+    // 5. write the runs out: consecutive sorted positions are consecutive
+    //    output positions within a digit's run
+    for (uint32_t q = threadIdx.x; q < valid; q += BT) {
         const uint32_t src = s_src[q];
-        const uint64_t g = (uint64_t)ws.counts[(uint64_t)dg * chunks + c] + (q - s_off[dg]);
-        for (uint32_t f = 0; f < d; ++f) P_out[(size_t)f * n + g] = __ldg(P + (size_t)f * n + c0 + src);
-        idx_out[g] = idx_in ? __ldg(idx_in + c0 + src) : (uint32_t)(c0 + src);
+        const uint32_t key = s_key[src];
+        const uint32_t g = s_base[(key >> shift) & (RADIX - 1u)] + q;
+        for (uint32_t f = 0; f < d; ++f) P_out[(size_t)f * n + g] = s_pts[(size_t)f * CH + src];
+        if (keys_out) keys_out[g] = (uint16_t)key;
+        if (idx_out) idx_out[g] = idx_in ? s_idx[src] : (uint32_t)(c0 + src);
     }
 }
 
-__global__ void __launch_bounds__(SB) unpermute_kernel(uint64_t n, const uint32_t* __restrict__ perm,
-                                                       const uint32_t* __restrict__ in, uint32_t* __restrict__ out) {
-    for (uint64_t q = (uint64_t)blockIdx.x * SB + threadIdx.x; q < n; q += (uint64_t)gridDim.x * SB)
+__global__ void __launch_bounds__(256) unpermute_kernel(uint64_t n, const uint32_t* __restrict__ perm,
+                                                        const uint32_t* __restrict__ in, uint32_t* __restrict__ out) {
+    for (uint64_t q = (uint64_t)blockIdx.x * 256 + threadIdx.x; q < n; q += (uint64_t)gridDim.x * 256)
         out[perm[q]] = in[q];
 }
 
 uint32_t grid_of(uint64_t n) {
-    uint64_t g = (n + SB - 1) / SB;
+    uint64_t g = (n + 255) / 256;
     const uint64_t cap = (uint64_t)device_info().sm_count * 8;
     if (g > cap) g = cap;
     return (uint32_t)(g < 1 ? 1 : g);
+}
+
+int scan_offsets(uint32_t* counts, uint32_t* partial, uint64_t chunks, cudaStream_t s) {
+    const uint64_t nblk = scan_blocks_of(chunks);
+    scan_partial_kernel<<<(unsigned)nblk, RADIX, 0, s>>>(counts, chunks, partial);
+    scan_top_kernel<<<1, RADIX, 0, s>>>(partial, (uint32_t)nblk);
+    scan_apply_kernel<<<(unsigned)nblk, RADIX, 0, s>>>(counts, chunks, partial, (uint32_t)nblk);
+    return 3;
+}
+
+template <uint32_t CH, int BT>
+int set_scatter_smem(uint32_t d) {
+    static bool done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && done[dev]) return CKM_OK;
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, scatter_kernel<CH, BT>);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(spatial scatter)");
+    if (fa.sharedSizeBytes + scatter_smem(d, true) > device_info().smem_optin)
+        return fail(CKM_ERR_UNSUPPORTED, "spatial sort: the scatter's staging buffers exceed shared memory");
+    e = cudaFuncSetAttribute(scatter_kernel<CH, BT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(device_info().smem_optin - fa.sharedSizeBytes));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(spatial scatter)");
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return CKM_OK;
+}
+
+template <uint32_t CH, int BT>
+int sort_passes(uint32_t d, uint64_t n, const float* points, float* sorted, uint32_t* perm, const SortWs& ws,
+                cudaStream_t s) {
+    int st = set_scatter_smem<CH, BT>(d);
+    if (st != CKM_OK) return st;
+    const uint64_t chunks = num_chunks(n, d);
+    // 16-byte copies and loads need 16-byte aligned rows: the base and n * 4
+    const int vec_in = ((reinterpret_cast<uintptr_t>(points) & 15u) == 0 && (n & 3u) == 0) ? 1 : 0;
+    const int vec_tmp = ((reinterpret_cast<uintptr_t>(ws.tmp_points) & 15u) == 0 && (n & 3u) == 0) ? 1 : 0;
+    uint64_t launches = 0;
+
+    const uint32_t samples = (uint32_t)std::min<uint64_t>(n, BBOX_SAMPLES);
+    const uint64_t stride = n / samples;
+    const unsigned bbox_grid = (unsigned)std::min<uint64_t>(256, (samples + 255) / 256);
+    bbox_sample_kernel<<<bbox_grid, 256, 0, s>>>(points, n, d, stride, samples, ws.lo, ws.hi);
+    launch_keys(d, chunks, points, n, ws.lo, ws.hi, vec_in, ws.keys0, ws.counts, s);
+    launches += 2 + scan_offsets(ws.counts, ws.partial, chunks, s);
+    scatter_kernel<CH, BT><<<(unsigned)chunks, BT, scatter_smem(d, false), s>>>(
+        points, nullptr, ws.keys0, n, d, 0, ws.counts, vec_in, ws.tmp_points, ws.keys1, perm ? ws.tmp_idx : nullptr);
+    hist_kernel<CH, BT><<<(unsigned)chunks, BT, 0, s>>>(ws.keys1, n, 8, ws.counts);
+    launches += 2 + scan_offsets(ws.counts, ws.partial, chunks, s);
+    scatter_kernel<CH, BT><<<(unsigned)chunks, BT, scatter_smem(d, perm != nullptr), s>>>(
+        ws.tmp_points, perm ? ws.tmp_idx : nullptr, ws.keys1, n, d, 8, ws.counts, vec_tmp, sorted, nullptr, perm);
+    launches += 1;
+    count_launch(launches);
+    return CKM_OK;
 }
 
 }  // namespace
 
 size_t spatial_sort_workspace_bytes(uint64_t n, uint32_t d) {
     if (d == 0) return 0;
-    return 256 + a256((size_t)RADIX * num_chunks(n, d) * 4) + a256((size_t)scan_blocks_of(n, d) * 4) +
-           a256((size_t)n * d * 4) + a256((size_t)n * 4);
+    const WsSizes z = ws_sizes(n, d);
+    return 256 + z.counts + z.partial + 2 * z.keys + z.pts + z.idx;
 }
-
-namespace {
-size_t downsweep_smem(uint32_t d) { return (size_t)chunk_items(d) * 4; }  // s_src (u16) + two digit arrays
-}  // namespace
 
 int launch_spatial_sort(uint32_t d, uint64_t n, const float* points, float* sorted, uint32_t* perm, void* ws_ptr,
                         cudaStream_t s) {
@@ -377,46 +597,17 @@ int launch_spatial_sort(uint32_t d, uint64_t n, const float* points, float* sort
     if (e == cudaSuccess) e = cudaMemsetAsync(ws.hi, 0, 16 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return cuda_fail(e, "spatial sort: workspace init");
     if (n == 0) return CKM_OK;
-    const uint32_t b = d >= 16 ? 1u : 16u / d;
-    const uint32_t chunk = chunk_items(d);
-    const uint64_t chunks = num_chunks(n, d);
-    const uint64_t m = (uint64_t)RADIX * chunks;
-    const uint64_t scan_blocks = scan_blocks_of(n, d);
-    const size_t smem = downsweep_smem(d);
-    static bool attr_done[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-        cudaFuncAttributes fa;
-        e = cudaFuncGetAttributes(&fa, downsweep_kernel);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes(spatial downsweep)");
-        e = cudaFuncSetAttribute(downsweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(device_info().smem_optin - fa.sharedSizeBytes));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(spatial downsweep)");
-        attr_done[dev] = true;
-    }
-    bbox_kernel<<<grid_of(n), SB, 0, s>>>(points, n, d, ws);
-    for (uint32_t pass = 0; pass < 2; ++pass) {
-        const uint32_t shift = 8 * pass;
-        const float* src = pass == 0 ? points : ws.tmp_points;
-        const uint32_t* src_idx = pass == 0 ? nullptr : ws.tmp_idx;
-        float* dst = pass == 0 ? ws.tmp_points : sorted;
-        uint32_t* dst_idx = pass == 0 ? ws.tmp_idx : perm;
-        upsweep_kernel<<<(unsigned)chunks, SB, 0, s>>>(src, n, d, b, ws, shift, chunk, chunks);
-        scan_sums_kernel<<<(unsigned)scan_blocks, SB, 0, s>>>(ws.counts, m, ws.block_sums);
-        scan_block_sums_kernel<<<1, 1024, 0, s>>>(ws.block_sums, (uint32_t)scan_blocks);
-        scan_apply_kernel<<<(unsigned)scan_blocks, SB, 0, s>>>(ws.counts, m, ws.block_sums);
-        downsweep_kernel<<<(unsigned)chunks, SB, smem, s>>>(src, src_idx, n, d, b, ws, shift, chunk, chunks, dst,
-                                                            dst_idx);
-    }
-    count_launch(11);
+    const int st = d <= 4 ? sort_passes<4096, SB>(d, n, points, sorted, perm, ws, s)
+                          : (d <= 8 ? sort_passes<2048, SB>(d, n, points, sorted, perm, ws, s)
+                                    : sort_passes<1024, SB>(d, n, points, sorted, perm, ws, s));
+    if (st != CKM_OK) return st;
     e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "spatial sort launch");
 }
 
 int launch_unpermute_u32(uint64_t n, const uint32_t* perm, const uint32_t* in, uint32_t* out, cudaStream_t s) {
     if (n == 0) return CKM_OK;
-    unpermute_kernel<<<grid_of(n), SB, 0, s>>>(n, perm, in, out);
+    unpermute_kernel<<<grid_of(n), 256, 0, s>>>(n, perm, in, out);
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "unpermute launch");

@@ -63,10 +63,14 @@ public:
             auto& dp = this->measurement->add_datapoint().set_name("SpatialSort");
             Event& ev = dp.add_event(queue_);
             sorted_points_.resize(n * d);
-            perm_.resize(n);
+            // the permutation is only needed to bring the labels back when
+            // the run can stop early (the last iteration of a full run labels
+            // the caller's order directly)
+            if (this->converge) perm_.resize(n);
             sort_ws_.resize(ckm_spatial_sort_workspace_bytes(n, (uint32_t)d));
             ckm_check(ckm_spatial_sort_f32((uint32_t)d, n, reinterpret_cast<const float*>(points_.data()),
-                                           reinterpret_cast<float*>(sorted_points_.data()), perm_.data(),
+                                           reinterpret_cast<float*>(sorted_points_.data()),
+                                           this->converge ? perm_.data() : nullptr,
                                            sort_ws_.data(), sort_ws_.size(), queue_.get()),
                       "SpatialSort");
             ev.record_end(queue_);

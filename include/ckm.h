@@ -112,10 +112,12 @@ int ckm_fused_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clust
 
 /* Spatially ordered point sets (no counterpart in the reference; a layout
  * of the same points).  ckm_spatial_sort_f32 writes a copy of the
- * column-major points in Z-order of 2^16 cells of their bounding box
- * (1 <= d <= 16, n < 2^32; a stable radix sort, so equal cells keep the
- * caller's order) and perm[q] = the caller's index of sorted point q.  Its
- * workspace holds one more copy of the points and indices:
+ * column-major points in Z-order of 2^16 cells of their bounding box, taken
+ * over a strided sample of 2^20 points (points outside it fall in the edge
+ * cells) (1 <= d <= 16, n < 2^32; a stable radix sort, so equal cells keep
+ * the caller's order) and, when perm is not NULL, perm[q] = the caller's
+ * index of sorted point q.  Its workspace holds one more copy of the points,
+ * two 16-bit keys per point and the indices:
  * ckm_spatial_sort_workspace_bytes(n, d) bytes.
  * ckm_fused_sorted_f32 is ckm_fused_f32 (same contract, same labels, masses
  * and centroids for the points it is given) that, for d <= 8 and k <= 32,

@@ -33,6 +33,17 @@ def test_spatial_sort_is_a_permutation(ckm, cuda):
         assert np.array_equal(S.cpu().numpy().reshape(d, n), X[:, pm]), (n, d)
 
 
+def test_spatial_sort_without_permutation(ckm, cuda):
+    """perm = NULL: the same sorted points, no indices moved."""
+    import torch
+    for n, d in [(50001, 4), (33333, 3), (30000, 8), (4096 * 3, 2)]:
+        P = blobs(n, d, 6, seed=n * d)
+        dP, S, perm = _sorted_set(ckm, cuda, P, n, d)
+        S2, none = ckm.spatial_sort(dP, n, d, with_perm=False)
+        torch.cuda.synchronize()
+        assert none is None and torch.equal(S, S2), (n, d)
+
+
 def test_spatial_sort_makes_warp_boxes_small(ckm, cuda):
     """After the sort, consecutive 256-point groups span a small part of the
     data's range (the property the pruning relies on)."""
