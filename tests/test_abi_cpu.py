@@ -65,7 +65,7 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
 
 
 def test_documented_run_config_layout_and_name_checks(ckm):
-    """The ctypes RunConfig of INTEGRATION.md over a plain CDLL handle: an
+    """The ctypes RunConfig layout a binding declares, over a plain CDLL handle: an
     unknown name in any field the pipeline uses is reported as
     CKM_ERR_UNKNOWN_STRATEGY naming it, before any device work (the
     reference's factories throw std::invalid_argument(strategy),

@@ -49,6 +49,38 @@ def test_three_stage_functors(ckm, oracle, cuda, n, d, k):
     check_centroids(oracle, P, n, d, k, ref, dS.cpu().numpy())
 
 
+@pytest.mark.parametrize("kind", ["f32", "f64", "u32", "u64"])
+def test_matrix_add_accumulates(ckm, cuda, kind):
+    """ckm_matrix_add_*: a += b elementwise (MatrixBinaryOp::matrix Add,
+    matrix_binary_op.hpp:149-188), the buffered strategies' accumulation of
+    per-chunk sums and masses; the integer forms wrap mod 2^32 / 2^64."""
+    import ctypes
+    import torch
+    rng = np.random.default_rng(11)
+    count = 100003
+    dt = {"f32": np.float32, "f64": np.float64, "u32": np.uint32, "u64": np.uint64}[kind]
+    if kind.startswith("f"):
+        a = rng.normal(size=count).astype(dt)
+        b = rng.normal(size=count).astype(dt)
+        want = a + b
+    else:
+        hi = 1 << (32 if kind == "u32" else 63)
+        a = rng.integers(0, hi, size=count, dtype=np.uint64).astype(dt)
+        b = rng.integers(0, hi, size=count, dtype=np.uint64).astype(dt)
+        want = a + b                       # numpy wraps like the device
+    view = {"u32": np.int32, "u64": np.int64}.get(kind, dt)
+    da = torch.from_numpy(a.view(view).copy()).to(cuda)
+    db = torch.from_numpy(b.view(view).copy()).to(cuda)
+    fn = getattr(ckm.lib(), "ckm_matrix_add_" + kind)
+    fn.argtypes = [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    s = torch.cuda.current_stream()
+    assert fn(count, da.data_ptr(), db.data_ptr(), s.cuda_stream) == 0
+    torch.cuda.synchronize()
+    got = da.cpu().numpy().view(dt)
+    assert np.array_equal(got, want)
+    assert fn(0, da.data_ptr(), db.data_ptr(), s.cuda_stream) == 0   # empty: no work, no error
+
+
 def test_mass_update_exact_uniform_labels(ckm, cuda):
     """The reference's histogram test (test/histogram.cpp:31-39, 211-226):
     exact counts of 1 Mi uniform labels for 2..16 bins."""
