@@ -568,19 +568,38 @@ def run_batched_only(args, ckm, torch, jobs, iters, total_pts, subset, stream):
     return 0
 
 
-def run_buffered_workload(args, ckm, torch, dev):
-    """Out-of-core Lloyd (config 2b, scaled to this box): n points of d = 16
-    from a 64-blob mixture (centres U[-10,10]^16, sigma U[0.5,2]) held in
-    PINNED HOST memory, k = 64, first_x initial centroids, run through the
-    buffered three-stage pipeline (ckm_kmeans_run_f32, three_stage_buffered)
-    with the device budget capped at a quarter of the point bytes (config 2b:
-    128 GiB of points, 32 GiB budget), so most chunks stream over the host
-    link every iteration.  Metric: pts*iter/s end to end (host points, device
-    compute, host labels)."""
-    n = args.buffered_points or (1 << 29)
+def host_mem_available():
+    """MemAvailable of this host in bytes (None if /proc/meminfo is unreadable)."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def buffered_record(ckm, torch, dev, n, budget, iters, steps):
+    """Out-of-core Lloyd (config 2b): n = 2^31 points of d = 16 from a 64-blob
+    mixture (centres U[-10,10]^16, sigma U[0.5,2]) held in PINNED HOST memory
+    (128 GiB), k = 64, first_x initial centroids, run through the buffered
+    three-stage pipeline (ckm_kmeans_run_f32, three_stage_buffered) with the
+    device budget capped at 32 GiB, so most chunks stream over the host link
+    every iteration; 50 iterations.  Metric: pts*iter/s end to end (host
+    points, device compute, host labels).  The host must hold the points and
+    labels pinned with room to spare: the run is refused, with the measured
+    figures, when MemAvailable is below that."""
     d, k, blobs = 16, 64, 64
-    iters = args.buffered_iterations
-    budget = args.buffered_budget or (n * d * 4) // 4
+    budget = budget or min((n * d * 4) // 4, 32 << 30)
+    need = n * d * 4 + n * 4
+    avail = host_mem_available()
+    margin = 24 << 30
+    if avail is not None and avail < need + margin:
+        return {"metric": "pts*iter/s", "unit": "pts*iter/s", "n_gpus": 1,
+                "config": {"workload": "buffered_three_stage_n%d_d%d_k%d" % (n, d, k)},
+                "unavailable": "host MemAvailable %.1f GiB < %.1f GiB of pinned points and labels + "
+                               "%.0f GiB margin" % (avail / 2 ** 30, need / 2 ** 30, margin / 2 ** 30)}
     # host points generated on the device in chunks of the same mixture
     P = torch.empty(n * d, dtype=torch.float32, pin_memory=True)
     L = torch.empty(n, dtype=torch.int32, pin_memory=True)
@@ -606,7 +625,7 @@ def run_buffered_workload(args, ckm, torch, dev):
 
     run(1)                          # warm-up: allocations, first chunks
     times, infos = [], []
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, min(steps, 3))
     for _ in range(steps):
         t, info, M = run(iters)
         times.append(t)
@@ -625,8 +644,16 @@ def run_buffered_workload(args, ckm, torch, dev):
         "h2d_gbs_effective": info.h2d_bytes / t / 1e9,
         "h2d_link_probe_gbs": link[0],
         "kernel_launches_per_step": int(info.kernel_launches),
+        "host_mem_available_gib": avail / 2 ** 30 if avail is not None else None,
     }
-    print(json.dumps(line), flush=True)
+    del P, L, Pn, Ln
+    return line
+
+
+def run_buffered_workload(args, ckm, torch, dev):
+    rec = buffered_record(ckm, torch, dev, args.buffered_points or (1 << 31), args.buffered_budget,
+                          args.buffered_iterations, args.steps)
+    print(json.dumps(rec), flush=True)
     return 0
 
 
@@ -949,10 +976,11 @@ def main():
     ap.add_argument("--no-plain", action="store_true",
                     help="batched workload: time the batched launches alone (no plain loop, no graph)")
     ap.add_argument("--tc-points", type=int, default=0, help="tensor_core workload: points (default 2^24)")
-    ap.add_argument("--buffered-points", type=int, default=0, help="buffered workload: points (default 2^29)")
+    ap.add_argument("--buffered-points", type=int, default=0, help="buffered workload: points (default 2^31)")
     ap.add_argument("--buffered-budget", type=int, default=0,
-                    help="buffered workload: device budget in bytes (default a quarter of the point bytes)")
-    ap.add_argument("--buffered-iterations", type=int, default=5, help="buffered workload: iterations per step")
+                    help="buffered workload: device budget in bytes (default a quarter of the point bytes, "
+                         "at most 32 GiB)")
+    ap.add_argument("--buffered-iterations", type=int, default=50, help="buffered workload: iterations per step")
     ap.add_argument("--no-simt-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1141,7 +1169,10 @@ def main():
         for name, fn in (("tensor_core", lambda: tensor_core_record(ckm, torch, dev, 1 << 24, 3, 3, fp64=fp64)),
                          ("batched", lambda: batched_record(ckm, torch, dev, 4096, 3, 3, fp64=fp64)),
                          ("serving", lambda: serving_record(ckm, torch, dev, 10.0, 2000.0, 0.5, 512, 100, 0,
-                                                            with_70pct=False, burst_rounds=2, fp64=fp64))):
+                                                            with_70pct=False, burst_rounds=2, fp64=fp64)),
+                         # config 2b at its size (2^31 x 16 pinned on the host, 32 GiB device
+                         # budget), 5 of its 50 iterations
+                         ("buffered", lambda: buffered_record(ckm, torch, dev, 1 << 31, 0, 5, 1))):
             try:
                 subs[name] = fn()
             except Exception as ex:  # report, keep the headline
