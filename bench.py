@@ -948,6 +948,122 @@ def tensor_core_record(ckm, torch, dev, n, steps, warmup, simt_compare=True, cpu
     }
 
 
+def _round_bf16(a):
+    """float32 -> nearest bfloat16 (ties to even), returned as float64."""
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _round_e4m3(a):
+    """float64 values already scaled into e4m3's range -> nearest e4m3 value
+    (3 mantissa bits, exponents -6..8, subnormal step 2^-9, max 448)."""
+    a = np.asarray(a, np.float64)
+    m, e = np.frexp(np.abs(a))                # |a| = m 2^e, m in [0.5, 1)
+    step = np.ldexp(1.0, np.maximum(e - 4, -9))
+    q = np.round(np.abs(a) / step) * step      # numpy rounds half to even
+    return np.sign(a) * np.minimum(q, 448.0)
+
+
+def precision_record(ckm, torch, dev, n, warm_iters=5, sample=4096):
+    """Candidate fractions of the tensor-core certificate per operand
+    precision, measured on the tensor-core workload (n points, d = 128,
+    k = 1024, the 1024-component mixture) with the centroids after
+    `warm_iters` real iterations of ckm_tc_fused_f32.  For each precision the
+    sample's operands are rounded as the kernel would round them, the scores
+    |c|^2 - 2 x.c are formed from the rounded operands, and the kernel's
+    certificate T = t1 |x| + te |e| + t2 (|x| + cm)^2 (with fm, e the measured
+    rounding-error norms of that precision) decides which clusters stay
+    candidates.  fp8 e4m3 gets a scale per point row and per centroid row
+    (at least as fine as per-tile scales); 'fp16 hi/lo' is the three-product
+    split x_h c_h + x_h c_l + x_l c_h.  The reference's FP32 label must be a
+    candidate in every case (soundness)."""
+    d, k = 128, 1024
+    P = torch.empty(n * d, dtype=torch.float32, device=dev)
+    ckm.generate_mixture_ex(P, n, d, k, SEED, center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0),
+                            dirichlet=True)
+    tcp = ckm.TensorCorePoints(P, n, d)
+    C = [P.view(d, n)[:, :k].reshape(-1).clone(), torch.empty(k * d, dtype=torch.float32, device=dev)]
+    L = torch.empty(n, dtype=torch.int32, device=dev)
+    M = torch.empty(k, dtype=torch.int32, device=dev)
+    S = ckm.new_scratch(d, k, dev)
+    stats = torch.zeros(2, dtype=torch.int32, device=dev)
+    for i in range(warm_iters):
+        ckm.tc_fused(P, tcp, C[i % 2], C[(i + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats)
+        if i == 0:
+            tcp.sort(k)
+    torch.cuda.synchronize()
+    Cc = C[warm_iters % 2].cpu().numpy()                       # column-major k x d
+    rng = np.random.default_rng(17)
+    idx = np.sort(rng.choice(n, size=sample, replace=False))
+    Xcm = np.ascontiguousarray(P.view(d, n)[:, torch.from_numpy(idx).to(dev)].cpu().numpy())
+    del P, tcp
+    torch.cuda.empty_cache()
+    O = oracle_module()
+    ref = O.label_f32(Xcm.reshape(-1), sample, d, k, Cc)
+    X = Xcm.T.astype(np.float64)                               # sample x d
+    Cr = Cc.reshape(d, k).T.astype(np.float64)                 # k x d
+    valid = np.all(np.isfinite(Cr), axis=1)
+    Cv = np.where(valid[:, None], Cr, 0.0)
+    cn2 = np.where(valid, (Cv * Cv).sum(1).astype(np.float32).astype(np.float64), np.inf)
+    xn = np.sqrt((X * X).sum(1))
+    cm = float(np.sqrt((Cv * Cv).sum(1)).max())
+    g = 2 * d * 2.0 ** -23
+    t2 = 2 * 2.0 ** -23 + 2 * (d + 2) * 2.0 ** -24
+
+    def pow2_scale(maxabs, top):
+        return np.ldexp(1.0, np.floor(np.log2(top / maxabs)).astype(int))
+
+    def rounded(kind):
+        if kind == "fp16":
+            sx = float(pow2_scale(np.abs(X).max(), 2.0 ** 15))
+            sc = float(pow2_scale(np.abs(Cv).max(), 2.0 ** 15))
+            return (X * sx).astype(np.float16).astype(np.float64) / sx, \
+                   (Cv * sc).astype(np.float16).astype(np.float64) / sc, 0.0
+        if kind == "bf16":
+            return _round_bf16(X), _round_bf16(Cv), 0.0
+        if kind == "fp8 e4m3":
+            sx = pow2_scale(np.maximum(np.abs(X).max(1), 1e-30), 448.0)[:, None]
+            sc = pow2_scale(np.maximum(np.abs(Cv).max(1), 1e-30), 448.0)[:, None]
+            return _round_e4m3(X * sx) / sx, _round_e4m3(Cv * sc) / sc, 0.0
+        # fp16 hi/lo: the x_l c_l product is dropped (|x_l||c_l| <= 2^-22 |x||c|)
+        sx = float(pow2_scale(np.abs(X).max(), 2.0 ** 15))
+        sc = float(pow2_scale(np.abs(Cv).max(), 2.0 ** 15))
+        xh = (X * sx).astype(np.float16).astype(np.float64)
+        ch = (Cv * sc).astype(np.float16).astype(np.float64)
+        xl = (X * sx - xh).astype(np.float16).astype(np.float64)
+        cl = (Cv * sc - ch).astype(np.float16).astype(np.float64)
+        return (xh + xl) / sx, (ch + cl) / sc, 2.0 ** -21
+
+    table = {}
+    for kind, mma_cost in (("fp16", 1.0), ("bf16", 1.0), ("fp8 e4m3", 0.5), ("fp16 hi/lo", 3.0)):
+        Xr, Cq, dropped = rounded(kind)
+        e = np.sqrt(((Xr - X) ** 2).sum(1))
+        fm = float(np.sqrt(((Cq - Cv) ** 2).sum(1))[valid].max())
+        t1 = 4 * fm + 4 * g * (cm + fm)
+        te = 4 * (cm + fm) + 4 * g * (cm + fm)
+        T = t1 * xn + te * e + (t2 + 2 * dropped) * (xn + cm) ** 2
+        scores = cn2[None, :] - 2.0 * (Xr @ Cq.T)
+        m = scores.min(1)
+        cand = scores <= (m + T)[:, None]
+        counts = cand.sum(1)
+        table[kind] = {"relative_mma_work": mma_cost, "median_T": float(np.median(T)),
+                       "points_with_2plus_candidates": float(np.mean(counts >= 2)),
+                       "mean_candidates": float(counts.mean()), "max_candidates": int(counts.max()),
+                       "points_over_8_candidates": float(np.mean(counts > 8)),
+                       "reference_label_always_a_candidate": bool(np.all(cand[np.arange(sample), ref]))}
+    return {"metric": "candidate fraction", "unit": "fraction of points", "n_gpus": 1,
+            "config": {"workload": "tensor_core_precision_table", "n": n, "d": d, "k": k,
+                       "centroids": "after %d iterations of ckm_tc_fused_f32 from the first k points" % warm_iters,
+                       "sample_points": sample},
+            "precisions": table}
+
+
+def run_precision_workload(args, ckm, torch, dev):
+    print(json.dumps(precision_record(ckm, torch, dev, args.tc_points or (1 << 24))), flush=True)
+    return 0
+
+
 def run_tensor_core_workload(args, ckm, torch, dev):
     rec = tensor_core_record(ckm, torch, dev, args.tc_points or (1 << 24), args.steps, args.warmup,
                              simt_compare=not args.no_simt_compare, cpu_baseline=not args.no_cpu_baseline)
@@ -961,7 +1077,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core", "serving", "buffered"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batched", "tensor_core", "serving", "buffered",
+                                                                   "precision"])
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving: small jobs per second")
     ap.add_argument("--serve-large-rate", type=float, default=0.5, help="serving: large jobs per second")
@@ -996,13 +1113,14 @@ def main():
     if args.impl == "reference":
         return run_reference_arm(args, workload if workload in WORKLOADS else DEFAULT_WORKLOAD)
 
-    if workload in ("batched", "tensor_core", "serving", "buffered"):
+    if workload in ("batched", "tensor_core", "serving", "buffered", "precision"):
         import importlib
 
         import torch
         ckm = importlib.import_module("cl-kmeans_gb300")
         run = {"batched": run_batched_workload, "tensor_core": run_tensor_core_workload,
-               "serving": run_serving_workload, "buffered": run_buffered_workload}[workload]
+               "serving": run_serving_workload, "buffered": run_buffered_workload,
+               "precision": run_precision_workload}[workload]
         return run(args, ckm, torch, torch.device("cuda", 0))
 
     import importlib
