@@ -842,7 +842,8 @@ def run_serving_workload(args, ckm, torch, dev):
     return 0
 
 
-def tensor_core_record(ckm, torch, dev, n, steps, warmup, simt_compare=True, cpu_baseline=True, fp64=True):
+def tensor_core_record(ckm, torch, dev, n, steps, warmup, simt_compare=True, cpu_baseline=True, fp64=True,
+                       precision="fp16"):
     """Tensor-core labeling with precision recovery: n = 2^24, d = 128,
     k = 1024, a 1024-component mixture (centres ~ N(0, 4 I), sigma
     log-uniform in [0.25, 1], Dirichlet(1) weights), 20 fixed iterations.
@@ -854,7 +855,7 @@ def tensor_core_record(ckm, torch, dev, n, steps, warmup, simt_compare=True, cpu
     P = torch.empty(n * d, dtype=torch.float32, device=dev)
     ckm.generate_mixture_ex(P, n, d, k, SEED, center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0),
                             dirichlet=True)
-    tcp = ckm.TensorCorePoints(P, n, d)
+    tcp = ckm.TensorCorePoints(P, n, d, precision=precision)
     C = [P.view(d, n)[:, :k].reshape(-1).clone(), torch.empty(k * d, dtype=torch.float32, device=dev)]
     C0 = C[0].clone()
     L = torch.empty(n, dtype=torch.int32, device=dev)
@@ -929,7 +930,7 @@ def tensor_core_record(ckm, torch, dev, n, steps, warmup, simt_compare=True, cpu
     return {
         "metric": "pts*iter/s", "value": n / step_s, "unit": "pts*iter/s", "n_gpus": 1, "steps": steps,
         "warmup": warm, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp16 distances (tcgen05), f32 exact candidates, f64 sums",
+        "vs_baseline": None, "dtype": "%s distances (tcgen05), f32 exact candidates, f64 sums" % precision,
         "data": "synthetic (seeded 1024-component mixture generated on the device)",
         "config": {"workload": "lloyd_tc_n%d_d%d_k%d" % (n, d, k), "n": n, "d": d, "k": k,
                    "centres": "N(0, 4I)", "sigma": "log-uniform [0.25, 1]", "weights": "Dirichlet(1)",
@@ -1066,7 +1067,8 @@ def run_precision_workload(args, ckm, torch, dev):
 
 def run_tensor_core_workload(args, ckm, torch, dev):
     rec = tensor_core_record(ckm, torch, dev, args.tc_points or (1 << 24), args.steps, args.warmup,
-                             simt_compare=not args.no_simt_compare, cpu_baseline=not args.no_cpu_baseline)
+                             simt_compare=not args.no_simt_compare, cpu_baseline=not args.no_cpu_baseline,
+                             precision=args.tc_precision)
     print(json.dumps(rec), flush=True)
     return 0
 
@@ -1093,6 +1095,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true",
                     help="batched workload: time the batched launches alone (no plain loop, no graph)")
     ap.add_argument("--tc-points", type=int, default=0, help="tensor_core workload: points (default 2^24)")
+    ap.add_argument("--tc-precision", default="fp16", choices=["fp16", "bf16"],
+                    help="tensor_core workload: operand type of the distance GEMM")
     ap.add_argument("--buffered-points", type=int, default=0, help="buffered workload: points (default 2^31)")
     ap.add_argument("--buffered-budget", type=int, default=0,
                     help="buffered workload: device budget in bytes (default a quarter of the point bytes, "
@@ -1285,6 +1289,9 @@ def main():
         torch.cuda.empty_cache()
         fp64 = not args.no_fp64_check
         for name, fn in (("tensor_core", lambda: tensor_core_record(ckm, torch, dev, 1 << 24, 3, 3, fp64=fp64)),
+                         ("tensor_core_bf16", lambda: tensor_core_record(ckm, torch, dev, 1 << 24, 3, 3,
+                                                                         simt_compare=False, cpu_baseline=False,
+                                                                         fp64=fp64, precision="bf16")),
                          ("batched", lambda: batched_record(ckm, torch, dev, 4096, 3, 3, fp64=fp64)),
                          ("serving", lambda: serving_record(ckm, torch, dev, 10.0, 2000.0, 0.5, 512, 100, 0,
                                                             with_70pct=False, burst_rounds=2, fp64=fp64)),

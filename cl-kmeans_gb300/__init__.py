@@ -421,6 +421,8 @@ _TC_SIGS = {
     "ckm_tc_supported": ([ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     "ckm_tc_prepare_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                ctypes.c_void_p], ctypes.c_int),
+    "ckm_tc_prepare_points_ex": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "ckm_tc_counters": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "ckm_tc_sort_points": ([ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
                             ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),
@@ -447,14 +449,15 @@ class TensorCorePoints:
     rows, norm bounds, point indices) and the per-(n, d, k) workspace; torch
     device memory."""
 
-    def __init__(self, points, n, d, stream=None):
+    def __init__(self, points, n, d, stream=None, precision="fp16"):
         import torch
         L = _tc_lib()
         self.n, self.d = n, d
         nbytes = int(L.ckm_tc_points_bytes(n, d))
         self.buf = torch.empty(nbytes, dtype=torch.uint8, device=points.device)
-        check(L.ckm_tc_prepare_points(d, n, _p(points), _p(self.buf), nbytes, _stream(stream)),
-              "ckm_tc_prepare_points")
+        prec = {"fp16": 0, "bf16": 1}[precision]
+        check(L.ckm_tc_prepare_points_ex(d, n, _p(points), _p(self.buf), nbytes, prec, _stream(stream)),
+              "ckm_tc_prepare_points_ex")
         self.ws = {}
 
     def sort(self, k, stream=None):

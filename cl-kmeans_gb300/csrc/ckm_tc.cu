@@ -33,6 +33,7 @@
 // warpgroups over double-buffered tensor memory), exact recheck, offsets,
 // scatter, segmented sums, finalisation.
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -114,9 +115,24 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Instruction descriptor, kind::f16: D f32, A and B fp16, both K-major.
-__host__ __device__ __forceinline__ uint32_t idesc_f16_f32(uint32_t M, uint32_t N) {
-    return (1u << 4) | ((N >> 3) << 17) | ((M >> 4) << 24);
+// Instruction descriptor, kind::f16: D f32, A and B both fp16 or both bf16
+// (operand format 0 or 1 in the A and B format fields), both K-major.
+__host__ __device__ __forceinline__ uint32_t idesc_f16_f32(uint32_t M, uint32_t N, uint32_t precision = 0) {
+    const uint32_t ab = precision == CKM_TC_BF16 ? (1u << 7) | (1u << 10) : 0u;
+    return (1u << 4) | ab | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+// One operand value rounded to the point set's 2-byte type (fp16 or bf16):
+// the stored bits and the rounded value back in FP32.
+__device__ __forceinline__ uint16_t round_operand(float v, uint32_t precision, float& back) {
+    if (precision == CKM_TC_BF16) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        back = __bfloat162float(h);
+        return *reinterpret_cast<const uint16_t*>(&h);
+    }
+    const __half h = __float2half_rn(v);
+    back = __half2float(h);
+    return *reinterpret_cast<const uint16_t*>(&h);
 }
 
 // 32 consecutive accumulator columns of this thread's TMEM lane (no wait).
@@ -180,11 +196,12 @@ __global__ void __launch_bounds__(256) tc_points_maxabs_kernel(const float* __re
 __global__ void __launch_bounds__(256) tc_points_convert_kernel(const float* __restrict__ P, uint64_t n, uint32_t d,
                                                                 uint32_t d_pad, uint32_t d4,
                                                                 const TcPointsHeader* __restrict__ hdr,
-                                                                __half* __restrict__ ph, float* __restrict__ norms,
+                                                                uint16_t* __restrict__ ph, float* __restrict__ norms,
                                                                 float* __restrict__ errn, float* __restrict__ prm,
                                                                 uint32_t* __restrict__ orig) {
     extern __shared__ float s_tile[];  // [d][33]
     const float sx = ldexpf(1.0f, scale_exponent(__uint_as_float(hdr->maxabs_bits)));
+    const uint32_t prec = hdr->precision;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint64_t p0 = (uint64_t)blockIdx.x * 32; p0 < n; p0 += (uint64_t)gridDim.x * 32) {
         const uint64_t p = p0 + lane;
@@ -197,9 +214,9 @@ __global__ void __launch_bounds__(256) tc_points_convert_kernel(const float* __r
             for (uint32_t f = lane; f < d_pad; f += 32) {
                 const float v = f < d ? s_tile[f * 33 + r] : 0.0f;
                 ss = fmaf(v, v, ss);
-                const __half h = __float2half_rn(v * sx);
-                ph[q * d_pad + f] = h;
-                const float e = __half2float(h) - v * sx;  // exact: both within a factor 2 (or e = -v sx)
+                float back;
+                ph[q * d_pad + f] = round_operand(v * sx, prec, back);
+                const float e = back - v * sx;  // exact: both within a factor 2 (or e = -v sx)
                 ee = fmaf(e, e, ee);
             }
             for (uint32_t f = lane; f < d4; f += 32) prm[q * d4 + f] = f < d ? s_tile[f * 33 + r] : 0.0f;
@@ -258,22 +275,24 @@ __global__ void tc_centroid_stats_kernel(const float* __restrict__ C, uint32_t k
     }
 }
 
-// fp16 centroids scaled by sc, K-major [k_pad][d_pad] (invalid and padding
-// rows zero), and a bound of the fp16 rounding error of the valid rows.
+// Centroids scaled by sc in the point set's operand type (fp16 or bf16),
+// K-major [k_pad][d_pad] (invalid and padding rows zero), and a bound of the
+// rounding error of the valid rows.
 __global__ void tc_centroid_pack_kernel(const float* __restrict__ C, uint32_t k, uint32_t d, uint32_t k_pad,
-                                        uint32_t d_pad, const float* __restrict__ cn2, __half* __restrict__ ch,
-                                        TcIterDev* it) {
+                                        uint32_t d_pad, const float* __restrict__ cn2, uint16_t* __restrict__ ch,
+                                        const TcPointsHeader* __restrict__ hdr, TcIterDev* it) {
     const int ec = scale_exponent(__uint_as_float(it->cabs_bits));
     const float sc = ldexpf(1.0f, ec);
+    const uint32_t prec = hdr->precision;
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < k_pad; c += gridDim.x * blockDim.x) {
         const bool valid = c < k && cn2[c] < __int_as_float(0x7f800000);
-        __half* row = ch + (uint64_t)c * d_pad;
+        uint16_t* row = ch + (uint64_t)c * d_pad;
         double ee = 0.0;
         for (uint32_t f = 0; f < d_pad; ++f) {
             const float b = (valid && f < d) ? C[(uint64_t)f * k + c] * sc : 0.0f;
-            const __half h = __float2half_rn(b);
-            row[f] = h;
-            const double e = (double)__half2float(h) - (double)b;
+            float back;
+            row[f] = round_operand(b, prec, back);
+            const double e = (double)back - (double)b;
             ee = fma(e, e, ee);
         }
         if (valid)
@@ -313,6 +332,7 @@ struct LabelParams {
     const float* errn;           // upper bound of |fp16(x sx) / sx - x| per point
     const float* x_rm;           // FP32 points, row-major [n][d4]
     const uint32_t* orig;        // caller's index of each point of the set
+    const uint32_t* precision;   // the point set's operand type (its header)
     const float* c_rm;           // FP32 centroids, row-major [k][d4]
     const float* cn2;            // |c|^2 [k_pad]
     TcIterDev* it;
@@ -436,7 +456,7 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
         }
     } else if (warp == MMA_WARP) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_f16_f32(TILE_M, BN);
+            const uint32_t idesc = idesc_f16_f32(TILE_M, BN, *prm.precision);
             uint32_t ia = 0, ib = 0, ic = 0;
             bool ok = true;
             for (uint32_t q = blockIdx.x; ok && q < prm.num_pairs; q += gridDim.x, ++ia) {
@@ -1221,18 +1241,21 @@ bool tc_supported(uint32_t d, uint32_t k) {
     return label_cfg(d_pad, label_bn(d_pad), label_ctas_per_sm(d_pad), 1024, CN_SMEM_MAX * sizeof(float)).ok;
 }
 
-int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, cudaStream_t s) {
+int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, int precision, cudaStream_t s) {
     const TcLayout L = tc_layout(n, d, 1);
     char* b = static_cast<char*>(tc_points);
     TcPointsHeader* hdr = reinterpret_cast<TcPointsHeader*>(b);
-    // header, fp16 rows and norms start zeroed: padding rows stay zero
+    // header, 2-byte operand rows and norms start zeroed: padding rows stay zero
     cudaError_t e = cudaMemsetAsync(b, 0, L.pts_rm_off, s);
+    // the operand type (0 or 1) in the header's low byte of `precision`
+    if (e == cudaSuccess && precision)
+        e = cudaMemsetAsync(reinterpret_cast<char*>(&hdr->precision), precision, 1, s);
     if (e != cudaSuccess) return cuda_fail(e, "tc_prepare_points memset");
     if (n == 0) return CKM_OK;
     tc_points_maxabs_kernel<<<grid_for_n(n * d, 256, 8), 256, 0, s>>>(P, n * d, hdr);
     count_launch();
     tc_points_convert_kernel<<<grid_for_n(n, 32, 16), 256, (size_t)d * 33 * sizeof(float), s>>>(
-        P, n, d, L.d_pad, L.d4, hdr, reinterpret_cast<__half*>(b + L.pts_half_off),
+        P, n, d, L.d_pad, L.d4, hdr, reinterpret_cast<uint16_t*>(b + L.pts_half_off),
         reinterpret_cast<float*>(b + L.pts_norm_off), reinterpret_cast<float*>(b + L.pts_err_off),
         reinterpret_cast<float*>(b + L.pts_rm_off), reinterpret_cast<uint32_t*>(b + L.pts_orig_off));
     count_launch();
@@ -1309,7 +1332,7 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
     char* ws = static_cast<char*>(a.workspace);
     TcIterDev* it = reinterpret_cast<TcIterDev*>(ws);
     float* cent_rm = reinterpret_cast<float*>(ws + L.ws_cent_rm_off);
-    __half* cent_half = reinterpret_cast<__half*>(ws + L.ws_cent_half_off);
+    uint16_t* cent_half = reinterpret_cast<uint16_t*>(ws + L.ws_cent_half_off);
     float* cn2 = reinterpret_cast<float*>(ws + L.ws_cn2_off);
     uint32_t* flagged = reinterpret_cast<uint32_t*>(ws + L.ws_flagged_off);
     uint32_t* off = reinterpret_cast<uint32_t*>(ws + L.ws_off_off);
@@ -1323,7 +1346,8 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
     const int cgrid = (int)((L.k_pad + 255) / 256);
     tc_centroid_stats_kernel<<<cgrid, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d4, cent_rm, cn2, it);
     count_launch();
-    tc_centroid_pack_kernel<<<cgrid, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d_pad, cn2, cent_half, it);
+    tc_centroid_pack_kernel<<<cgrid, 256, 0, s>>>(a.centroids, a.k, a.d, L.k_pad, L.d_pad, cn2, cent_half,
+                                                  reinterpret_cast<const TcPointsHeader*>(pb), it);
     count_launch();
     tc_params_kernel<<<1, 1, 0, s>>>(a.d, L.d_pad, reinterpret_cast<const TcPointsHeader*>(pb), it);
     count_launch();
@@ -1335,6 +1359,7 @@ int tc_iteration(const TcArgs& a, cudaStream_t s) {
         prm.errn = reinterpret_cast<const float*>(pb + L.pts_err_off);
         prm.x_rm = reinterpret_cast<const float*>(pb + L.pts_rm_off);
         prm.orig = reinterpret_cast<const uint32_t*>(pb + L.pts_orig_off);
+        prm.precision = &reinterpret_cast<const TcPointsHeader*>(pb)->precision;
         prm.slabels = slabels;
         prm.res_pts = reinterpret_cast<uint32_t*>(ws + L.ws_res_pts_off);
         prm.res_cands = reinterpret_cast<uint32_t*>(ws + L.ws_res_cands_off);

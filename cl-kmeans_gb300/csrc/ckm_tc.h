@@ -12,7 +12,8 @@ namespace ckm {
 // Header at the start of a prepared point set (device memory, 256 bytes).
 struct TcPointsHeader {
     unsigned int maxabs_bits;  // max |x_f| over the finite coordinates (float bits)
-    uint32_t reserved[63];
+    uint32_t precision;        // operand type of the distance GEMM: CKM_TC_FP16 or CKM_TC_BF16
+    uint32_t reserved[62];
 };
 
 // Per-iteration device values (start of the workspace, 256 bytes).
@@ -61,7 +62,7 @@ struct TcArgs {
     int mode;
 };
 
-int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, cudaStream_t s);
+int tc_prepare_points(const float* P, uint64_t n, uint32_t d, void* tc_points, int precision, cudaStream_t s);
 // dst = src reordered by the label order of the last iteration run with `workspace`
 int tc_sort_points(uint64_t n, uint32_t d, uint32_t k, const void* src, void* dst, const void* workspace,
                    cudaStream_t s);

@@ -14,13 +14,20 @@ size_t ckm_tc_workspace_bytes(uint64_t n, uint32_t d, uint32_t k) { return tc_la
 
 int ckm_tc_supported(uint32_t d, uint32_t k) { return tc_supported(d, k) ? 1 : 0; }
 
-int ckm_tc_prepare_points(uint32_t d, uint64_t n, const float* points, void* tc_points, size_t bytes,
-                          ckm_stream_t stream) {
+int ckm_tc_prepare_points_ex(uint32_t d, uint64_t n, const float* points, void* tc_points, size_t bytes,
+                             int precision, ckm_stream_t stream) {
     if (d == 0) return fail(CKM_ERR_INVALID_ARGUMENT, "num_features must be >= 1");
     if (!tc_points || (n > 0 && !points)) return fail(CKM_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (precision != CKM_TC_FP16 && precision != CKM_TC_BF16)
+        return fail(CKM_ERR_INVALID_ARGUMENT, "precision must be CKM_TC_FP16 or CKM_TC_BF16");
     if (bytes < ckm_tc_points_bytes(n, d)) return fail(CKM_ERR_SCRATCH_TOO_SMALL, "tc_points smaller than ckm_tc_points_bytes");
     if (reinterpret_cast<uintptr_t>(tc_points) % 256) return fail(CKM_ERR_INVALID_ARGUMENT, "tc_points must be 256-byte aligned");
-    return tc_prepare_points(points, n, d, tc_points, (cudaStream_t)stream);
+    return tc_prepare_points(points, n, d, tc_points, precision, (cudaStream_t)stream);
+}
+
+int ckm_tc_prepare_points(uint32_t d, uint64_t n, const float* points, void* tc_points, size_t bytes,
+                          ckm_stream_t stream) {
+    return ckm_tc_prepare_points_ex(d, n, points, tc_points, bytes, CKM_TC_FP16, stream);
 }
 
 int ckm_tc_sort_points(uint32_t d, uint64_t n, uint32_t k, const void* tc_points, void* sorted_tc_points,

@@ -174,6 +174,16 @@ size_t ckm_tc_workspace_bytes(uint64_t num_points, uint32_t num_features, uint32
 int ckm_tc_supported(uint32_t num_features, uint32_t num_clusters);
 int ckm_tc_prepare_points(uint32_t num_features, uint64_t num_points, const float *points, void *tc_points,
                           size_t tc_points_bytes, ckm_stream_t stream);
+/* The same with the operand type of the distance GEMM chosen: CKM_TC_FP16
+ * (the default: fp16 operands scaled by powers of two) or CKM_TC_BF16.  The
+ * certificate is built from the operands' measured rounding errors, so both
+ * give the reference's labels; bf16's coarser rounding leaves more points to
+ * the exact resolution (a slower iteration on typical data).  Same functor
+ * as ckm_tc_prepare_points (fused_factory.hpp:34-53). */
+#define CKM_TC_FP16 0
+#define CKM_TC_BF16 1
+int ckm_tc_prepare_points_ex(uint32_t num_features, uint64_t num_points, const float *points, void *tc_points,
+                             size_t tc_points_bytes, int precision, ckm_stream_t stream);
 /* Diagnostics of the last ckm_tc_fused_f32 call made with `workspace`:
  * copies to the device array counters[4] (stream-ordered) the number of
  * points sent to the full exact recheck, the error flag, the number of

@@ -1,8 +1,8 @@
-"""Tensor-core fused iteration (ckm_tc_fused_f32): bf16 distances on
+"""Tensor-core fused iteration (ckm_tc_fused_f32): fp16 (or bf16) distances on
 tcgen05 with certified labels and exact FP32 recheck of near-ties.  The
 labels must be bit-exact against the oracle's restatement of the reference
 arithmetic (kmeans_naive.cpp:48-63) -- the certificate plus recheck is what
-makes a bf16 GEMM give reference labels -- masses exact, centroids within
+makes a 16-bit GEMM give reference labels -- masses exact, centroids within
 the fused tolerance of the FP64 means."""
 import numpy as np
 import pytest
@@ -13,10 +13,10 @@ from test_fused_gpu import check_centroids, to_dev
 pytestmark = pytest.mark.gpu
 
 
-def run_tc(ckm, cuda, P, n, d, k, C, iters=1):
+def run_tc(ckm, cuda, P, n, d, k, C, iters=1, precision="fp16"):
     import torch
     dP = to_dev(P, cuda)
-    tcp = ckm.TensorCorePoints(dP, n, d)
+    tcp = ckm.TensorCorePoints(dP, n, d, precision=precision)
     bufs = [to_dev(C, cuda), torch.zeros(k * d, dtype=torch.float32, device=cuda)]
     dL = torch.zeros(n, dtype=torch.int32, device=cuda)
     dM = torch.zeros(k, dtype=torch.int32, device=cuda)
@@ -39,14 +39,18 @@ def check_iter(oracle, P, n, d, k, Cin, lab, mass, Cout):
     check_centroids(oracle, P, n, d, k, ref, Cout)
 
 
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
 @pytest.mark.parametrize("n,d,k,iters", [(20000, 128, 1024, 2), (9999, 64, 300, 3), (5000, 100, 50, 3),
                                          (3000, 256, 256, 2), (4097, 32, 40, 3)])
-def test_tc_lockstep_matches_oracle(ckm, oracle, cuda, n, d, k, iters):
+def test_tc_lockstep_matches_oracle(ckm, oracle, cuda, n, d, k, iters, precision):
+    """fp16 and bf16 operands: either way the certificate (built from the
+    operands' measured rounding errors) and the exact resolution give the
+    reference's labels."""
     if not ckm.tc_supported(d, k):
         pytest.skip("tensor-core path not supported on this device")
     P = blobs(n, d, max(2, k // 4), seed=n + d + k, spread=4.0, sigma=0.5)
     C0 = oracle.first_x_f32(P, n, d, k)
-    for Cin, lab, mass, Cout, st in run_tc(ckm, cuda, P, n, d, k, C0, iters):
+    for Cin, lab, mass, Cout, st in run_tc(ckm, cuda, P, n, d, k, C0, iters, precision):
         assert st[1] == 0, "device wait ran out"
         check_iter(oracle, P, n, d, k, Cin, lab, mass, Cout)
 
