@@ -221,12 +221,28 @@ __device__ __forceinline__ uint32_t z_key(const float (&v)[D], const float* s_lo
     return key;
 }
 
-// Warp-aggregated count of one digit per lane into a shared histogram.
-__device__ __forceinline__ void count_digit(uint32_t* s_hist, uint32_t dg, bool ok) {
-    const uint32_t active = __ballot_sync(0xffffffffu, ok);
-    if (ok) {
-        const uint32_t peers = __match_any_sync(active, dg);
-        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_hist[dg], (uint32_t)__popc(peers));
+// Chunk histograms are counted in per-warp shared tables with plain integer
+// atomics (exact and order-independent), then summed per digit: warps never
+// contend with each other, and lanes of one warp that meet on a digit are
+// serialised by the atomic unit itself.
+template <int BT>
+struct WarpHist {
+    uint32_t h[BT / 32][RADIX];
+};
+
+template <int BT>
+__device__ __forceinline__ void hist_clear(WarpHist<BT>& wh) {
+    for (uint32_t i = threadIdx.x; i < (BT / 32) * RADIX; i += BT) (&wh.h[0][0])[i] = 0u;
+}
+
+// counts[chunk][digit] = the sum of the warps' tables (after a barrier).
+template <int BT>
+__device__ __forceinline__ void hist_store(const WarpHist<BT>& wh, uint32_t* __restrict__ counts) {
+    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < BT / 32; ++w) t += wh.h[w][j];
+        counts[(uint64_t)blockIdx.x * RADIX + j] = t;
     }
 }
 
@@ -243,10 +259,11 @@ __global__ void __launch_bounds__(BT) key_kernel(const float* __restrict__ P, ui
     constexpr uint32_t IPT = CH / BT;
     static_assert(IPT % 4 == 0 || IPT == 2, "4-point groups per thread");
     constexpr uint32_t B = D >= 16 ? 1u : 16u / D;
-    __shared__ uint32_t s_hist[RADIX];
+    __shared__ WarpHist<BT> s_wh;
     __shared__ float s_lo[16], s_scale[16];
     load_range(lo_w, hi_w, D, B, s_lo, s_scale);
-    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) s_hist[j] = 0u;
+    hist_clear(s_wh);
+    uint32_t* my_hist = s_wh.h[threadIdx.x >> 5];
     const uint64_t c0 = (uint64_t)blockIdx.x * CH;
     const bool seq = vec && IPT % 4 == 0;  // thread's points consecutive
     float v[IPT][D];
@@ -276,10 +293,10 @@ __global__ void __launch_bounds__(BT) key_kernel(const float* __restrict__ P, ui
         const uint64_t p = seq ? c0 + (uint64_t)IPT * threadIdx.x + r : c0 + r * BT + threadIdx.x;
         const uint32_t key = p < n ? z_key<D>(v[r], s_lo, s_scale) : 0u;
         keys[p] = (uint16_t)key;
-        count_digit(s_hist, key & (RADIX - 1u), p < n);
+        if (p < n) atomicAdd(&my_hist[key & (RADIX - 1u)], 1u);
     }
     __syncthreads();
-    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) counts[(uint64_t)blockIdx.x * RADIX + j] = s_hist[j];
+    hist_store(s_wh, counts);
 }
 
 template <int D>
@@ -306,9 +323,10 @@ template <uint32_t CH, int BT>
 __global__ void __launch_bounds__(BT) hist_kernel(const uint16_t* __restrict__ keys, uint64_t n, uint32_t shift,
                                                   uint32_t* __restrict__ counts) {
     constexpr uint32_t IPT = CH / BT;  // 8, 4 or 2 consecutive keys per thread: one 16, 8 or 4-byte load
-    __shared__ uint32_t s_hist[RADIX];
-    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) s_hist[j] = 0u;
+    __shared__ WarpHist<BT> s_wh;
+    hist_clear(s_wh);
     __syncthreads();
+    uint32_t* my_hist = s_wh.h[threadIdx.x >> 5];
     const uint64_t p0 = (uint64_t)blockIdx.x * CH + threadIdx.x * IPT;
     uint16_t k[IPT];
     if constexpr (IPT == 8) {
@@ -332,9 +350,10 @@ __global__ void __launch_bounds__(BT) hist_kernel(const uint16_t* __restrict__ k
         k[1] = (uint16_t)(v >> 16);
     }
 #pragma unroll
-    for (uint32_t r = 0; r < IPT; ++r) count_digit(s_hist, ((uint32_t)k[r] >> shift) & (RADIX - 1u), p0 + r < n);
+    for (uint32_t r = 0; r < IPT; ++r)
+        if (p0 + r < n) atomicAdd(&my_hist[((uint32_t)k[r] >> shift) & (RADIX - 1u)], 1u);
     __syncthreads();
-    for (uint32_t j = threadIdx.x; j < RADIX; j += BT) counts[(uint64_t)blockIdx.x * RADIX + j] = s_hist[j];
+    hist_store(s_wh, counts);
 }
 
 // --- exclusive scan of counts[chunk][digit] in digit-major order ----------
