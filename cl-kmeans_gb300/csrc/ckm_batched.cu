@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -529,6 +530,95 @@ int launch_batch_sync(const BatchJobDev* jobs, uint32_t num_jobs, cudaStream_t s
     count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CKM_OK : cuda_fail(e, "batch sync launch");
+}
+
+}  // namespace ckm
+
+// ----------------------------------------------------------------------------
+// The fused functor's tensor-core route: one job on the batched kernel.
+// ----------------------------------------------------------------------------
+namespace ckm {
+namespace {
+
+// Layout of the scratch extension (FUSED_UMMA_EXT bytes): the job record,
+// its status, tile ticket and work counter, then the segment list.
+constexpr size_t FU_JOB = 0, FU_STATUS = 128, FU_TICKET = 144, FU_WORK = 148, FU_SEGS = 256;
+constexpr uint32_t FU_MAX_SEGS = (uint32_t)((FUSED_UMMA_EXT - FU_SEGS) / sizeof(BatchSegment));
+constexpr uint32_t FU_TILE = 4096;
+// Where the route pays (measured per call against rows_kernel's TF32 mma.sync
+// screen, 20 calls each): at n = 2^20 with k = 256 it takes 603 against 786 us
+// (d = 64) and 344 against 391 us (d = 32); at k = 64 or n <= 2^18 rows_kernel
+// is faster (a 4096-point tile per segment leaves most SMs idle on small n,
+// and each segment restages the centroids).
+constexpr uint64_t FU_MIN_POINTS = 1ull << 20;
+constexpr uint32_t FU_MIN_K = 128;
+
+__global__ void fused_umma_setup_kernel(unsigned char* ext, BatchJobDev job, uint32_t nsegs, uint32_t per) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *reinterpret_cast<BatchJobDev*>(ext + FU_JOB) = job;
+        BatchStatus st;
+        st.shift = 0.0f;
+        st.iterations = 0u;
+        st.parity = 0u;  // centroids in cent[0] (the old ones); the means go to cent[1]
+        st.flags = 0u;
+        *reinterpret_cast<BatchStatus*>(ext + FU_STATUS) = st;
+        *reinterpret_cast<unsigned int*>(ext + FU_TICKET) = 0u;
+        *reinterpret_cast<unsigned int*>(ext + FU_WORK) = 0u;
+    }
+    BatchSegment* segs = reinterpret_cast<BatchSegment*>(ext + FU_SEGS);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nsegs; i += gridDim.x * blockDim.x) {
+        BatchSegment sg;
+        sg.job = 0u;
+        sg.tile_begin = i * per;
+        sg.tile_end = min((i + 1u) * per, job.num_tiles);
+        sg.pad = 0u;
+        segs[i] = sg;
+    }
+}
+
+}  // namespace
+
+int launch_fused_umma(const FusedF32& a, cudaStream_t s) {
+    const char* env = std::getenv("CKM_FUSED_UMMA");  // tuning: "0" never, "1" at any n
+    const bool never = env && env[0] == '0', always = env && env[0] == '1';
+    const DeviceInfo& di = device_info();
+    if (never || a.mode != CKM_MODE_FINALIZE || !a.scratch.ext || di.cc_major != 10 || (a.d != 32 && a.d != 64) ||
+        a.k < UMMA_MIN_K || a.k > UMMA_MAX_K || a.n == 0 || (!always && (a.n < FU_MIN_POINTS || a.k < FU_MIN_K)))
+        return -1000;
+    const uint64_t num_tiles = (a.n + FU_TILE - 1) / FU_TILE;
+    if (num_tiles > 0xffffffffull) return -1000;
+    const uint32_t per = (uint32_t)((num_tiles + FU_MAX_SEGS - 1) / FU_MAX_SEGS);
+    const uint32_t nsegs = (uint32_t)((num_tiles + per - 1) / per);
+    // shared-memory caps as the batch schedule sets them for a tensor-core job
+    const size_t need_c = ((size_t)a.k * a.d + ((a.k + 3u) & ~3u)) * sizeof(float);
+    const size_t budget = std::min<size_t>(di.smem_optin - 1024, 200 * 1024);
+    const size_t cent_cap = std::min((need_c + 255) & ~size_t(255), budget / 2);
+    const size_t acc_cap = budget - cent_cap;
+    unsigned char* ext = a.scratch.ext;
+    BatchJobDev job;
+    std::memset(&job, 0, sizeof(job));
+    job.points = a.points;
+    job.cent[0] = const_cast<float*>(a.centroids);  // read only: the kernel writes cent[parity ^ 1]
+    job.cent[1] = a.new_centroids;
+    job.labels = a.labels;
+    job.masses = a.masses;
+    job.sums = a.scratch.sums;
+    job.msum = a.scratch.masses;
+    job.ticket = reinterpret_cast<unsigned int*>(ext + FU_TICKET);
+    job.status = reinterpret_cast<BatchStatus*>(ext + FU_STATUS);
+    job.n = a.n;
+    job.d = a.d;
+    job.k = a.k;
+    job.num_tiles = (uint32_t)num_tiles;
+    fused_umma_setup_kernel<<<1, 256, 0, s>>>(ext, job, nsegs, per);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "fused tensor-core setup launch");
+    const uint32_t grid = std::min<uint32_t>((uint32_t)di.sm_count, nsegs);
+    return launch_batched(reinterpret_cast<const BatchJobDev*>(ext + FU_JOB),
+                          reinterpret_cast<const BatchSegment*>(ext + FU_SEGS), nsegs,
+                          reinterpret_cast<unsigned int*>(ext + FU_WORK), 0.0f, 0u, grid, 512, FU_TILE, 16, cent_cap,
+                          acc_cap, 1u, s);
 }
 
 }  // namespace ckm

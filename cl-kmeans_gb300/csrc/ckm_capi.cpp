@@ -41,6 +41,11 @@ ScratchLayout scratch_layout(uint32_t d, uint32_t k) {
     L.mass_off = align256((size_t)d * k * sizeof(double));
     L.ctrl_off = L.mass_off + align256((size_t)k * sizeof(unsigned long long));
     L.total = L.ctrl_off + 256;
+    L.ext_off = 0;
+    if ((d == 32 || d == 64) && k >= 16 && k <= 256) {
+        L.ext_off = L.total;
+        L.total += FUSED_UMMA_EXT;
+    }
     return L;
 }
 
@@ -173,6 +178,9 @@ int ckm_fused_f32(uint32_t d, uint64_t n, uint32_t k, const float* points, const
                scratch_view(scratch, scratch_layout(d, k)), n, d, k, mode};
     cudaStream_t s = (cudaStream_t)stream;
     if (lowd_supported(d, k)) return launch_fused_f32(a, Pass::Fused, s);
+    // d = 32 / 64 with enough points: the tensor cores (tcgen05)
+    st = launch_fused_umma(a, s);
+    if (st != -1000) return st;
     return launch_generic_f32(a, Pass::Fused, s);
 }
 

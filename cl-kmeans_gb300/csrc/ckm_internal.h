@@ -20,8 +20,13 @@ int cuda_fail(cudaError_t err, const char* where);
 //   sums     double[k * d]   column-major like the centroids (f * k + c)
 //   masses   uint64[k]
 //   control  uint32[64]      [0] CTA arrival ticket, [1] error flag
+//   ext      FUSED_UMMA_EXT bytes, only for the shapes the fused call may run
+//            on the tensor cores (d = 32 / 64, 16 <= k <= 256): the one-job
+//            record, status, tile ticket, work counter and segment list of
+//            the batched kernel (ckm_batched.cu, launch_fused_umma)
+constexpr size_t FUSED_UMMA_EXT = 4096;
 struct ScratchLayout {
-    size_t sums_off, mass_off, ctrl_off, total;
+    size_t sums_off, mass_off, ctrl_off, ext_off, total;  // ext_off 0: no extension
 };
 ScratchLayout scratch_layout(uint32_t d, uint32_t k);
 
@@ -29,12 +34,14 @@ struct ScratchView {
     double* sums;
     unsigned long long* masses;
     unsigned int* ctrl;
+    unsigned char* ext;  // nullptr without the extension
 };
 inline ScratchView scratch_view(void* base, const ScratchLayout& L) {
     char* b = static_cast<char*>(base);
     return ScratchView{reinterpret_cast<double*>(b + L.sums_off),
                        reinterpret_cast<unsigned long long*>(b + L.mass_off),
-                       reinterpret_cast<unsigned int*>(b + L.ctrl_off)};
+                       reinterpret_cast<unsigned int*>(b + L.ctrl_off),
+                       L.ext_off ? reinterpret_cast<unsigned char*>(b + L.ext_off) : nullptr};
 }
 
 // Counts kernel launches made by this library (for the run info and bench).
@@ -86,6 +93,10 @@ enum class Pass { Fused, LabelOnly, SumsOnly };
 
 // Launchers (return CKM_OK or an error status; never throw).
 int launch_fused_f32(const FusedF32& a, Pass pass, cudaStream_t s);
+// The fused iteration (FINALIZE) of one d = 32 / 64 job on the batched
+// kernel's tensor-core path; -1000 when the shape, device or scratch does
+// not qualify (the caller takes another kernel).
+int launch_fused_umma(const FusedF32& a, cudaStream_t s);
 // Spatial order (ckm_spatial.cu): radix sort by a Z-order cell key.
 size_t spatial_sort_workspace_bytes(uint64_t n, uint32_t d);
 int launch_spatial_sort(uint32_t d, uint64_t n, const float* points, float* sorted, uint32_t* perm, void* ws,

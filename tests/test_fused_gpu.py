@@ -310,3 +310,70 @@ def test_invalid_arguments_are_rejected(ckm, cuda):
     with pytest.raises(ckm.CkmError) as e:
         ckm.fused(dP, dP, dP, dP, dP, small, 4, 4, 4)
     assert e.value.status == -3
+
+
+# d = 32 / 64, FINALIZE: ckm_fused_f32 runs one job on the batched kernel's
+# tensor-core path (tcgen05, certified screen, exact resolution of unproved
+# points) when n >= 2^20 and k >= 128; CKM_FUSED_UMMA=1 forces it at any n and
+# 16 <= k <= 256, =0 keeps the rows kernel.
+UMMA_ROUTE = [(1 << 20, 64, 128, None), (1 << 20, 32, 256, None), (100003, 32, 40, "1"), (70001, 64, 256, "1"),
+              (65536, 32, 16, "1"), (131072, 32, 255, "1")]
+
+
+@pytest.mark.parametrize("n,d,k,force", UMMA_ROUTE)
+def test_fused_tensor_core_route_matches_oracle(ckm, oracle, cuda, monkeypatch, n, d, k, force):
+    if force:
+        monkeypatch.setenv("CKM_FUSED_UMMA", force)
+    P = blobs(n, d, max(2, k // 2), seed=n + 31 * d + k)
+    C = oracle.first_x_f32(P, n, d, k)
+    newC, masses, labels, _ = run_fused_once(ckm, cuda, P, n, d, k, C)
+    ref = oracle.label_f32(P, n, d, k, C)
+    assert np.array_equal(labels, ref), "labels differ at %d points" % int((labels != ref).sum())
+    assert np.array_equal(masses, oracle.mass_u32(ref, k))
+    check_centroids(oracle, P, n, d, k, ref, newC)
+
+
+def test_fused_tensor_core_route_lockstep(ckm, oracle, cuda, monkeypatch):
+    """Several iterations on one scratch buffer: the route's records in the
+    scratch are rebuilt every call and its sums re-zeroed."""
+    import torch
+    monkeypatch.setenv("CKM_FUSED_UMMA", "1")
+    n, d, k, iters = 100000, 64, 96, 5
+    P = blobs(n, d, k, seed=17)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    dP = to_dev(P, cuda)
+    dC = [to_dev(C0, cuda), torch.zeros(k * d, dtype=torch.float32, device=cuda)]
+    dL = torch.zeros(n, dtype=torch.int32, device=cuda)
+    dM = torch.zeros(k, dtype=torch.int32, device=cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    for it in range(iters):
+        Cin = dC[it % 2].cpu().numpy()
+        ckm.fused(dP, dC[it % 2], dC[(it + 1) % 2], dL, dM, S, n, d, k, ckm.MODE_FINALIZE)
+        torch.cuda.synchronize()
+        ref = oracle.label_f32(P, n, d, k, Cin)
+        assert np.array_equal(dL.cpu().numpy().view(np.uint32), ref), "iteration %d" % it
+        assert np.array_equal(dM.cpu().numpy().view(np.uint32), oracle.mass_u32(ref, k))
+        check_centroids(oracle, P, n, d, k, ref, dC[(it + 1) % 2].cpu().numpy())
+    # the scratch is back to zero for the next caller (sums and masses)
+    assert not torch.any(S[:ckm.scratch_bytes(d, k) - 4096 - 256] != 0)
+
+
+@pytest.mark.parametrize("force", ["1", "0"])
+def test_fused_tensor_core_route_forced_ties_nan(ckm, oracle, cuda, monkeypatch, force):
+    """The route forced on at small n (CKM_FUSED_UMMA=1) and off (=0): exact
+    ties pick the lowest index and a NaN centroid never wins either way."""
+    monkeypatch.setenv("CKM_FUSED_UMMA", force)
+    for d, k in [(32, 40), (64, 17), (64, 256)]:
+        n = 6000
+        P = blobs(n, d, 6, seed=d + k)
+        C = oracle.first_x_f32(P, n, d, k).reshape(d, k)
+        C[:, 2] = C[:, 1]
+        C[:, 9] = C[:, 3]
+        C[:, 5] = np.nan
+        C = np.ascontiguousarray(C).reshape(-1)
+        newC, masses, labels, _ = run_fused_once(ckm, cuda, P, n, d, k, C)
+        ref = oracle.label_f32(P, n, d, k, C)
+        assert np.array_equal(labels, ref), (d, k, int((labels != ref).sum()))
+        assert not np.any(np.isin(labels, [2, 5, 9]))
+        assert np.array_equal(masses, oracle.mass_u32(ref, k))
+        check_centroids(oracle, P, n, d, k, ref, newC)
