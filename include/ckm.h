@@ -99,7 +99,12 @@ int ckm_scratch_init(void *scratch, size_t scratch_bytes, ckm_stream_t stream);
 /* Replaces FusedFactory::FusedFunction (fused_factory.hpp:34-53), i.e.     */
 /* FusedFeatureSum::operator() (cl_kernels/fused_feature_sum.hpp:191-444)   */
 /* and FusedClusterMerge::operator() (cl_kernels/fused_cluster_merge.hpp:   */
-/* 193-414).                                                                */
+/* 193-414).  ckm_fused_f32 picks its kernel by shape: d <= 16 the low-d    */
+/* kernel; d = 32 / 64 the rows kernel, or, in FINALIZE mode with k >= 128  */
+/* and n >= 2^20, one job of the batched kernel's tcgen05 path (its records */
+/* in a 4 KiB part of the scratch that ckm_scratch_bytes includes for       */
+/* d = 32 / 64 with 16 <= k <= 256); otherwise the generic kernel.  The     */
+/* labels are the reference's on every path.                                */
 /* ---------------------------------------------------------------------- */
 int ckm_fused_f32(uint32_t num_features, uint64_t num_points, uint32_t num_clusters,
                   const float *points, const float *old_centroids, float *new_centroids,
