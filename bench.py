@@ -1259,7 +1259,9 @@ def main():
                "total_time_window_ms": window_ms,
                "window_roofline_frac": bytes_per_point * n * iters_cfg / (window_ms / 1e3) / 1e9 / peak,
                "window": "the reference's TotalTime window (kmeans_single_stage.hpp:89-160): the spatial sort "
-                         "and all %d iterations" % iters_cfg}
+                         "and all %d iterations; window_roofline_frac counts the reference's 20 B per "
+                         "point-iteration, while the run's intermediate iterations on the sorted copy write no "
+                         "labels (nothing reads them: the last iteration labels the caller's order)" % iters_cfg}
         if not args.no_fp64_check and rank == 0:
             # the call's result against the FP64 oracle: centroids against the
             # FP64 means of the returned labels, masses against their counts

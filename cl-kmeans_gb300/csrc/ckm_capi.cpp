@@ -191,13 +191,15 @@ int ckm_fused_sorted_f32(uint32_t d, uint64_t n, uint32_t k, const float* points
     if (st) return st;
     if (!valid_mode(mode)) return fail(CKM_ERR_INVALID_ARGUMENT, "mode must be DEFER, FINALIZE or ACCUMULATE");
     if ((st = check_scratch(scratch, scratch_bytes, d, k))) return st;
-    if (n > 0 && (!points || !labels)) return fail(CKM_ERR_INVALID_ARGUMENT, "points/labels NULL");
+    // labels NULL: not written (the low-d kernel only; nothing reads them)
+    if (n > 0 && (!points || (!labels && !lowd_supported(d, k))))
+        return fail(CKM_ERR_INVALID_ARGUMENT, "points/labels NULL");
     if (!old_centroids) return fail(CKM_ERR_INVALID_ARGUMENT, "old_centroids NULL");
     if (mode != CKM_MODE_DEFER && (!new_centroids || !masses))
         return fail(CKM_ERR_INVALID_ARGUMENT, "new_centroids/masses NULL");
     FusedF32 a{points, old_centroids, labels, new_centroids, masses,
                scratch_view(scratch, scratch_layout(d, k)), n, d, k, mode};
-    a.flags = FUSED_BOX_PRUNE;
+    a.flags = FUSED_BOX_PRUNE | (labels ? 0u : FUSED_NO_LABELS);
     cudaStream_t s = (cudaStream_t)stream;
     if (lowd_supported(d, k)) return launch_fused_f32(a, Pass::Fused, s);
     return launch_generic_f32(a, Pass::Fused, s);

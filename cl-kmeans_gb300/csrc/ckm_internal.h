@@ -76,6 +76,9 @@ struct FusedF32 {
 };
 
 constexpr uint32_t FUSED_BOX_PRUNE = 1u;
+// FUSED_NO_LABELS: the low-d fused pass writes no labels (a caller whose
+// labels of this iteration nobody reads; the sums and masses are the same).
+constexpr uint32_t FUSED_NO_LABELS = 2u;
 
 struct FusedF64 {
     const double* points;

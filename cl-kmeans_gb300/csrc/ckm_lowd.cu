@@ -217,8 +217,9 @@ __device__ __forceinline__ void process_tile(Tile<D, PPT>& T, const FusedF32& a,
 #pragma unroll 2
             for (uint32_t c = 0; c < k; ++c, cp += D) dist_argmin<D, PPT>(T, best, cp, c);
         }
-        // labels out
-        if (vec && p0 + PPT <= n) {
+        // labels out (unless the caller reads none this iteration)
+        if (a.flags & FUSED_NO_LABELS) {
+        } else if (vec && p0 + PPT <= n) {
 #pragma unroll
             for (int v = 0; v < PPT; v += VW) {
                 if constexpr (VW == 4) {

@@ -86,11 +86,14 @@ public:
                 Event& ev = dp.add_event(queue_);
                 Scratch& sc = engine_.scratch();
                 sc.reserve((uint32_t)d, (uint32_t)k, queue_);
+                // a run that cannot stop early reads none of these labels
+                // (its last iteration labels the caller's order): skip them
                 ckm_check(ckm_fused_sorted_f32((uint32_t)d, n, (uint32_t)k,
                                                reinterpret_cast<const float*>(iter_points),
                                                reinterpret_cast<const float*>(centroids_.data()),
                                                reinterpret_cast<float*>(new_centroids_.data()),
-                                               reinterpret_cast<uint32_t*>(labels_.data()),
+                                               this->converge ? reinterpret_cast<uint32_t*>(labels_.data())
+                                                              : nullptr,
                                                reinterpret_cast<uint32_t*>(masses_.data()), sc.data(), sc.bytes(),
                                                CKM_MODE_FINALIZE, queue_.get()),
                           "FusedFeatureSumSorted");

@@ -129,7 +129,10 @@ int ckm_fused_f64(uint32_t num_features, uint64_t num_points, uint32_t num_clust
  * skips per warp the clusters provably farther than another from all of the
  * warp's points; on a spatially ordered set most clusters are skipped.  Its
  * labels follow the order of the points it is given; ckm_unpermute_u32
- * brings them to the caller's order (out[perm[q]] = in[q]). */
+ * brings them to the caller's order (out[perm[q]] = in[q]).  For d <= 16,
+ * labels may be NULL: none are written (an iteration whose labels nobody
+ * reads, e.g. every iteration but the last of a fixed-length run); masses
+ * and centroids are unchanged. */
 size_t ckm_spatial_sort_workspace_bytes(uint64_t num_points, uint32_t num_features);
 int ckm_spatial_sort_f32(uint32_t num_features, uint64_t num_points, const float *points, float *sorted_points,
                          uint32_t *perm, void *workspace, size_t workspace_bytes, ckm_stream_t stream);

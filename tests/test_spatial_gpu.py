@@ -126,3 +126,28 @@ def test_spatial_rejects_bad_arguments(ckm, cuda):
         ckm.spatial_sort(t, 4, 17)       # d > 16
     L = ckm.lib()
     assert L.ckm_spatial_sort_f32(4, 16, t.data_ptr(), t.data_ptr(), t.data_ptr(), t.data_ptr(), 16, None) != 0
+
+
+def test_fused_sorted_without_labels(ckm, oracle, cuda):
+    """labels = NULL: no labels written, the same masses and centroids (the
+    strategies' intermediate iterations on a sorted copy)."""
+    import torch
+    n, d, k = 1 << 17, 4, 16
+    P = blobs(n, d, 16, seed=21)
+    dP, S, perm = _sorted_set(ckm, cuda, P, n, d)
+    C0 = oracle.first_x_f32(P, n, d, k)
+    out = []
+    for with_labels in (True, False):
+        dC = to_dev(C0, cuda)
+        dN = torch.zeros(k * d, dtype=torch.float32, device=cuda)
+        dL = torch.full((n,), -1, dtype=torch.int32, device=cuda)
+        dM = torch.zeros(k, dtype=torch.int32, device=cuda)
+        sc = ckm.new_scratch(d, k, cuda)
+        ckm.fused_sorted(S, dC, dN, dL if with_labels else None, dM, sc, n, d, k, ckm.MODE_FINALIZE)
+        torch.cuda.synchronize()
+        out.append((dN.cpu().numpy(), dM.cpu().numpy(), dL.cpu().numpy()))
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert np.all(out[1][2] == -1)                      # untouched
+    ref = oracle.label_f32(P, n, d, k, C0)
+    assert np.array_equal(out[0][2].view(np.uint32), ref[perm.cpu().numpy().view(np.uint32)])
