@@ -32,6 +32,7 @@
 // (persistent, warp-specialised: TMA producer warp, MMA warp, two epilogue
 // warpgroups over double-buffered tensor memory), exact recheck, offsets,
 // scatter, segmented sums, finalisation.
+#include <cooperative_groups.h>
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -40,6 +41,8 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "ckm_device.cuh"
@@ -113,6 +116,18 @@ __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volati
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// counts[c] += 1 for every calling thread, with one atomic per distinct c
+// among the calling threads of a warp.  In a cluster-ordered point set the
+// points of a warp, and those that all SMs label at the same time, mostly
+// share one or two labels: one atomic per point would serialise at those
+// few counters.
+__device__ __forceinline__ void count_label(uint32_t* counts, uint32_t c) {
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    const cg::coalesced_group same = cg::labeled_partition(g, c);
+    if (same.thread_rank() == 0) atomicAdd(&counts[c], same.size());
 }
 
 // Instruction descriptor, kind::f16: D f32, A and B both fp16 or both bf16
@@ -627,7 +642,7 @@ __global__ void __launch_bounds__(LABEL_THREADS, 1)
                 } else {
                     prm.labels[__ldg(prm.orig + p)] = label;
                     prm.slabels[p] = label;
-                    atomicAdd(&prm.counts[label], 1u);
+                    count_label(prm.counts, label);
                 }
             }
             const unsigned int novf = __popc(__ballot_sync(0xffffffffu, valid && ovf));
@@ -713,7 +728,7 @@ __global__ void __launch_bounds__(256) tc_resolve_kernel(const float* __restrict
         } else {
             labels[__ldg(orig + p)] = bi;
             slabels[p] = bi;
-            atomicAdd(&counts[bi], 1u);
+            count_label(counts, bi);
         }
     }
 }
@@ -813,7 +828,7 @@ __global__ void __launch_bounds__(256) tc_recheck_kernel(const float* __restrict
             const uint32_t p = flagged[q0 + i];
             labels[orig[p]] = lab;
             slabels[p] = lab;
-            atomicAdd(&counts[lab], 1u);
+            count_label(counts, lab);
         }
         __syncthreads();
     }
@@ -1167,7 +1182,19 @@ LabelCfg label_cfg(uint32_t d_pad, uint32_t bn, uint32_t ctas, size_t static_sme
     const size_t budget = limit - static_smem - 1024;  // 1024: alignment of the swizzled tiles
     const size_t lists = (size_t)(CAP + 1) * EPI_THREADS * 8 + extra;
     const size_t a = (size_t)PAIR_M * d_pad * 2, b = (size_t)bn * d_pad * 2;
-    const uint32_t tries[][2] = {{2, 4}, {2, 3}, {2, 2}, {1, 4}, {1, 3}, {1, 2}, {1, 1}};
+    uint32_t tries[8][2] = {{2, 4}, {2, 3}, {2, 2}, {1, 4}, {1, 3}, {1, 2}, {1, 1}, {1, 1}};
+    // tuning: CKM_TC_STAGES="a,b" tries that depth first
+    const char* env = std::getenv("CKM_TC_STAGES");
+    unsigned ea = 0, eb = 0;
+    if (env && std::sscanf(env, "%u,%u", &ea, &eb) == 2 && ea >= 1 && ea <= MAX_A_STAGES && eb >= 1 &&
+        eb <= MAX_B_STAGES) {
+        for (int i = 7; i > 0; --i) {
+            tries[i][0] = tries[i - 1][0];
+            tries[i][1] = tries[i - 1][1];
+        }
+        tries[0][0] = ea;
+        tries[0][1] = eb;
+    }
     for (const auto& t : tries) {
         const size_t need = t[0] * a + t[1] * b + lists;
         if (need <= budget) {
