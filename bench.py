@@ -1103,7 +1103,7 @@ def main():
                          "at most 32 GiB)")
     ap.add_argument("--buffered-iterations", type=int, default=50, help="buffered workload: iterations per step")
     ap.add_argument("--no-simt-compare", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-spatial", action="store_true",
                     help="default workload: time the caller's point order only (no spatial sort, no box pruning)")
@@ -1249,11 +1249,15 @@ def main():
                                                    hostC.data_ptr(), hostM.data_ptr(), hostL.data_ptr(),
                                                    ctypes.byref(info)), "ckm_kmeans_run_f32")
             times.append(time.perf_counter() - t0)
-        e2e_t = statistics.mean(times[1:])
+        # the median call: the host link and the host's memory are shared with
+        # the box's other GPUs, and a call now and then takes 2-4x longer
+        e2e_t = statistics.median(times[1:])
         window_ms = info.total_time_ns / 1e6
         e2e = {"value": n * iters_cfg / e2e_t, "unit": "pts*iter/s",
                "h2d_bytes_per_step": int(info.h2d_bytes), "d2h_bytes_per_step": int(info.d2h_bytes),
                "iterations_per_step": iters_cfg, "ms_per_step": e2e_t * 1e3,
+               "statistic": "median of %d calls after the first" % (len(times) - 1),
+               "ms_per_step_mean": statistics.mean(times[1:]) * 1e3,
                "ms_per_call": [t * 1e3 for t in times],
                "first_call": "allocates the device buffers from the stream-ordered pool; not in ms_per_step",
                "total_time_window_ms": window_ms,
