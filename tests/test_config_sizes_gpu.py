@@ -19,6 +19,9 @@ an FP64 oracle.
   size-independent properties: both orders give the same masses and
   centroids, the masses sum to n, and a 2^20-point sample of the labels equals
   the oracle's.
+* Tensor-core Lloyd at its size (n = 2^24, d = 128, k = 1024): two
+  iterations, a 16384-point sample of the labels against the oracle, masses
+  against the label counts, centroids against the FP64 means of the labels.
 """
 import numpy as np
 import pytest
@@ -137,3 +140,53 @@ def test_config2a_full_size_properties(ckm, oracle, cuda):
     # the same labels: the FP64-merged sums of the two orders round to FP32 at
     # most one ulp apart
     assert np.all(np.abs(c_c - c_s) <= np.spacing(np.abs(c_c)))
+
+
+def test_config3_full_size_sample_and_properties(ckm, oracle, cuda):
+    """Config 3 at its size: n = 2^24, d = 128, k = 1024 (1024-component
+    mixture, centres N(0, 4I), sigma log-U[0.25, 1], Dirichlet(1) weights),
+    two tensor-core iterations (ckm_tc_fused_f32, fp16 operands) from the
+    first-k centroids, the prepared set sorted by label after the first as
+    the benchmark runs it.  Per iteration: the labels of a 16384-point sample
+    equal the oracle's from the same input centroids, the masses equal the
+    label counts, and the centroids of the non-empty clusters are within 1e-6
+    (normwise relative) of the FP64 means of their points under the returned
+    labels; the empty ones are NaN."""
+    import torch
+    n, d, k = 1 << 24, 128, 1024
+    if not ckm.tc_supported(d, k):
+        pytest.skip("tensor-core path not supported on this device")
+    P = torch.empty(n * d, dtype=torch.float32, device=cuda)
+    ckm.generate_mixture_ex(P, n, d, k, 42, center=("normal", 0.0, 2.0), sigma=("loguniform", 0.25, 1.0),
+                            dirichlet=True)
+    Pv = P.view(d, n)
+    tcp = ckm.TensorCorePoints(P, n, d)
+    C = [Pv[:, :k].reshape(-1).clone(), torch.empty(k * d, dtype=torch.float32, device=cuda)]
+    L = torch.empty(n, dtype=torch.int32, device=cuda)
+    M = torch.empty(k, dtype=torch.int32, device=cuda)
+    S = ckm.new_scratch(d, k, cuda)
+    stats = torch.zeros(2, dtype=torch.int32, device=cuda)
+    idx = np.sort(np.random.default_rng(11).choice(n, size=1 << 14, replace=False))
+    Xs = np.ascontiguousarray(Pv[:, torch.from_numpy(idx).to(cuda)].cpu().numpy()).reshape(-1)
+    for it in range(2):
+        Cin = C[it % 2].cpu().numpy()
+        ckm.tc_fused(P, tcp, C[it % 2], C[(it + 1) % 2], L, M, S, n, d, k, ckm.MODE_FINALIZE, stats)
+        torch.cuda.synchronize()
+        assert int(stats[1].item()) == 0, "device wait ran out"
+        lab = L.cpu().numpy().view(np.uint32)
+        ref = oracle.label_f32(Xs, len(idx), d, k, Cin)
+        assert np.array_equal(lab[idx], ref), "iteration %d: %d sample labels differ" % (
+            it, int((lab[idx] != ref).sum()))
+        counts = torch.bincount(L.long(), minlength=k)
+        assert torch.equal(M.long(), counts)
+        sums = torch.zeros(k, d, dtype=torch.float64, device=cuda)
+        for s0 in range(0, n, 1 << 22):
+            sums.index_add_(0, L[s0:s0 + (1 << 22)].long(), Pv[:, s0:s0 + (1 << 22)].t().double())
+        full = counts > 0
+        means = sums[full] / counts[full].double()[:, None]
+        got = C[(it + 1) % 2].view(d, k).t().double()[full]
+        rel = parity.rel_centroid_error(got.cpu().numpy(), means.cpu().numpy())
+        assert rel <= 1e-6, "iteration %d: relative centroid error %.3g" % (it, rel)
+        assert torch.isnan(C[(it + 1) % 2].view(d, k).t()[~full]).all()
+        if it == 0:
+            tcp.sort(k)
