@@ -22,6 +22,9 @@ an FP64 oracle.
 * Tensor-core Lloyd at its size (n = 2^24, d = 128, k = 1024): two
   iterations, a 16384-point sample of the labels against the oracle, masses
   against the label counts, centroids against the FP64 means of the labels.
+* Batched jobs at their size (4096 jobs, 196 M points): one step, every
+  job's masses and centroids against its labels in FP64, every 64th job's
+  labels against the oracle.
 """
 import numpy as np
 import pytest
@@ -190,3 +193,51 @@ def test_config3_full_size_sample_and_properties(ckm, oracle, cuda):
         assert torch.isnan(C[(it + 1) % 2].view(d, k).t()[~full]).all()
         if it == 0:
             tcp.sort(k)
+
+
+def test_config4_full_size_lockstep(ckm, oracle, cuda):
+    """Batched jobs at their size: 4096 jobs (n log-U[2^10, 2^18], d from
+    {2, 8, 32, 64}, k log-U[4, 256] with k <= n/16, each its own mixture of k
+    blobs with centres U[-10, 10]^d and sigma 1, the first k points as initial
+    centroids) in one batch, one step.  Every job: masses equal its label
+    counts, centroids within 1e-5 (normwise relative) of the FP64 means of its
+    labels, empty clusters NaN; every 64th job: labels equal the oracle's."""
+    import torch
+    rng = np.random.default_rng(1234)
+    jobs = []
+    for j in range(4096):
+        n = int(round(np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 18)))))
+        d = int(rng.choice([2, 8, 32, 64]))
+        k = int(round(np.exp(rng.uniform(np.log(4), np.log(256)))))
+        k = max(1, min(k, n // 16))
+        P = torch.empty(n * d, dtype=torch.float32, device=cuda)
+        ckm.generate_mixture(P, n, d, k, 1234 + j, sigma=(1.0, 1.0))
+        C0 = P.view(d, n)[:, :k].reshape(-1).clone()
+        jobs.append(dict(points=P, centroids=C0.clone(), init=C0,
+                         labels=torch.empty(n, dtype=torch.int32, device=cuda),
+                         masses=torch.empty(k, dtype=torch.int32, device=cuda), n=n, d=d, k=k))
+    b = ckm.Batch(jobs)
+    try:
+        b.step()
+        b.sync()
+        torch.cuda.synchronize()
+        worst = 0.0
+        for i, j in enumerate(jobs):
+            n, d, k = j["n"], j["d"], j["k"]
+            L = j["labels"].long()
+            counts = torch.bincount(L, minlength=k)
+            assert torch.equal(j["masses"].long(), counts), (i, n, d, k)
+            sums = torch.zeros(k, d, dtype=torch.float64, device=cuda)
+            sums.index_add_(0, L, j["points"].view(d, n).t().double())
+            full = counts > 0
+            means = sums[full] / counts[full].double()[:, None]
+            Ck = j["centroids"].view(d, k).t()
+            worst = max(worst, parity.rel_centroid_error(Ck.double()[full].cpu().numpy(), means.cpu().numpy()))
+            assert torch.isnan(Ck[~full]).all(), (i, n, d, k)
+            if i % 64 == 0:
+                ref = oracle.label_f32(j["points"].cpu().numpy(), n, d, k, j["init"].cpu().numpy())
+                lab = j["labels"].cpu().numpy().view(np.uint32)
+                assert np.array_equal(lab, ref), (i, n, d, k, int((lab != ref).sum()))
+        assert worst <= 1e-5, worst
+    finally:
+        b.close()
