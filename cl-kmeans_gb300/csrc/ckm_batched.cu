@@ -133,6 +133,42 @@ __device__ __forceinline__ void run_tiles_fixed(const BatchJobDev& J, uint32_t t
     }
 }
 
+// run_tiles_fixed for D <= 16 with two points per thread (p and p + BT):
+// each centroid row read from shared memory serves both, and the two points'
+// chains run side by side.  Labels and sums per point as run_tiles_fixed.
+template <int D, int BT>
+__device__ __forceinline__ void run_tiles_fixed2(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile,
+                                                 const float* s_c, const float* s_cn, float cm, float* s_sum,
+                                                 unsigned int* s_mass, uint32_t copies) {
+    const uint64_t n = J.n;
+    const uint32_t k = J.k;
+    const float* __restrict__ P = J.points;
+    const uint64_t hi = min((uint64_t)t1 * tile, n);
+    for (uint64_t p = (uint64_t)t0 * tile + threadIdx.x; p < hi; p += 2 * BT) {
+        const uint64_t q = p + BT;
+        const bool vq = q < hi;
+        float xa[D], xb[D];
+#pragma unroll
+        for (int f = 0; f < D; ++f) {
+            xa[f] = __ldg(P + (size_t)f * n + p);
+            xb[f] = vq ? __ldg(P + (size_t)f * n + q) : xa[f];
+        }
+        uint32_t la, lb;
+        if constexpr (Screened<D>::value) label_rows_screened2<D>(xa, xb, s_c, s_cn, cm, k, la, lb);
+        else label_rows_exact2<D>(xa, xb, s_c, k, la, lb);
+        J.labels[p] = la;
+#pragma unroll
+        for (int f = 0; f < D; ++f) add_feature(J, s_sum, copies, f, la, xa[f]);
+        add_mass(J, s_mass, copies, la);
+        if (vq) {
+            J.labels[q] = lb;
+#pragma unroll
+            for (int f = 0; f < D; ++f) add_feature(J, s_sum, copies, f, lb, xb[f]);
+            add_mass(J, s_mass, copies, lb);
+        }
+    }
+}
+
 template <int BT>
 __device__ __forceinline__ void run_tiles_generic(const BatchJobDev& J, uint32_t t0, uint32_t t1, uint32_t tile, const float* s_c,
                                   bool cent_smem, float* s_sum, unsigned int* s_mass, uint32_t copies, int parity) {
@@ -403,10 +439,10 @@ __global__ void __launch_bounds__(BT, 512 / BT) batched_kernel(const BatchJobDev
                 else run_tiles_mma<64, BT>(J, t, te, tile, reinterpret_cast<const float4*>(s_c), s_cn, cm, s_sum, s_mass, copies);
             } else if (cent_smem) {
                 switch (d) {
-                    case 2: run_tiles_fixed<2, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
-                    case 4: run_tiles_fixed<4, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
-                    case 8: run_tiles_fixed<8, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
-                    case 16: run_tiles_fixed<16, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 2: run_tiles_fixed2<2, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 4: run_tiles_fixed2<4, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 8: run_tiles_fixed2<8, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
+                    case 16: run_tiles_fixed2<16, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
                     case 32: run_tiles_fixed<32, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
                     case 64: run_tiles_fixed<64, BT>(J, t, te, tile, s_c, s_cn, cm, s_sum, s_mass, copies); break;
                     default: run_tiles_generic<BT>(J, t, te, tile, s_c, true, s_sum, s_mass, copies, parity); break;

@@ -152,6 +152,68 @@ __device__ __forceinline__ uint32_t label_rows_exact(const float (&x)[D], const 
     return lab;
 }
 
+// label_rows_exact for two points at once: each centroid row is read once
+// for both, and the two points' chains run side by side.  Each point gets
+// the arithmetic and the scan order of label_rows_exact.
+template <int D>
+__device__ __forceinline__ void label_rows_exact2(const float (&xa)[D], const float (&xb)[D],
+                                                  const float* __restrict__ cs, uint32_t k, uint32_t& la,
+                                                  uint32_t& lb) {
+    constexpr int VW = (D % 4 == 0) ? 4 : ((D % 2 == 0) ? 2 : 1);
+    constexpr int CB = 4;
+    float besta = FLT_MAX, bestb = FLT_MAX;
+    la = 0;
+    lb = 0;
+    uint32_t c = 0;
+    for (; c + CB <= k; c += CB) {
+        const float* r = cs + (size_t)c * D;
+        float acca[CB], accb[CB];
+#pragma unroll
+        for (int f = 0; f < D; f += VW) {
+#pragma unroll
+            for (int j = 0; j < CB; ++j) {
+                float cv[VW];
+                load_shared_vec<VW>(cv, r + j * D + f);
+#pragma unroll
+                for (int v = 0; v < VW; ++v) {
+                    const float ta = xa[f + v] - cv[v];
+                    const float tb = xb[f + v] - cv[v];
+                    acca[j] = (f + v == 0) ? ta * ta : fmaf(ta, ta, acca[j]);
+                    accb[j] = (f + v == 0) ? tb * tb : fmaf(tb, tb, accb[j]);
+                }
+            }
+        }
+        argmin_step2(besta, la, acca[0], acca[1], c);
+        argmin_step2(besta, la, acca[2], acca[3], c + 2u);
+        argmin_step2(bestb, lb, accb[0], accb[1], c);
+        argmin_step2(bestb, lb, accb[2], accb[3], c + 2u);
+    }
+    for (; c < k; ++c) {
+        const float* r = cs + (size_t)c * D;
+        float acca = 0.0f, accb = 0.0f;
+#pragma unroll
+        for (int f = 0; f < D; f += VW) {
+            float cv[VW];
+            load_shared_vec<VW>(cv, r + f);
+#pragma unroll
+            for (int v = 0; v < VW; ++v) {
+                const float ta = xa[f + v] - cv[v];
+                const float tb = xb[f + v] - cv[v];
+                acca = (f + v == 0) ? ta * ta : fmaf(ta, ta, acca);
+                accb = (f + v == 0) ? tb * tb : fmaf(tb, tb, accb);
+            }
+        }
+        if (acca < besta) {
+            besta = acca;
+            la = c;
+        }
+        if (accb < bestb) {
+            bestb = accb;
+            lb = c;
+        }
+    }
+}
+
 // Certified screen in front of label_rows_exact (D % 4 == 0).
 //
 // Score s_c = |c|^2 - 2 x.c: the dot product runs as two packed FP32 chains
@@ -228,6 +290,71 @@ __device__ __forceinline__ uint32_t label_rows_screened(const float (&x)[D], con
     const bool proved = (m1 < INFINITY) && (m2 - m1 > T) && (r * r < 0x1p120f);
     if (proved) return i1;
     return label_rows_exact<D>(x, cs, k);
+}
+
+// label_rows_screened for two points at once (each centroid row read once
+// for both); an unproved point gets label_rows_exact on its own.
+template <int D>
+__device__ __forceinline__ void label_rows_screened2(const float (&xa)[D], const float (&xb)[D],
+                                                     const float* __restrict__ cs, const float* __restrict__ cn,
+                                                     float cm, uint32_t k, uint32_t& la, uint32_t& lb) {
+    static_assert(D % 4 == 0, "screened rows need D % 4 == 0");
+    constexpr int CB = 4;
+    float2 nxa = make_float2(0.0f, 0.0f), nxb = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int f = 0; f < D; f += 2) {
+        nxa = fma2(make_float2(xa[f], xa[f + 1]), make_float2(xa[f], xa[f + 1]), nxa);
+        nxb = fma2(make_float2(xb[f], xb[f + 1]), make_float2(xb[f], xb[f + 1]), nxb);
+    }
+    const float ra = (sqrtf(nxa.x + nxa.y) * (1.0f + 0x1p-16f) + cm) * (1.0f + 0x1p-20f);
+    const float rb = (sqrtf(nxb.x + nxb.y) * (1.0f + 0x1p-16f) + cm) * (1.0f + 0x1p-20f);
+    const float Ta = fmaf((float)(4 * D + 32) * 0x1p-24f * ra, ra, 0x1p-126f) * 1.001f;
+    const float Tb = fmaf((float)(4 * D + 32) * 0x1p-24f * rb, rb, 0x1p-126f) * 1.001f;
+
+    float m1a = INFINITY, m2a = INFINITY, m1b = INFINITY, m2b = INFINITY;
+    uint32_t i1a = 0, i1b = 0;
+    uint32_t c = 0;
+    for (; c + CB <= k; c += CB) {
+        const float* row = cs + (size_t)c * D;
+        float2 acca[CB], accb[CB];
+#pragma unroll
+        for (int j = 0; j < CB; ++j) {
+            acca[j] = make_float2(0.0f, 0.0f);
+            accb[j] = make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int f = 0; f < D; f += 4) {
+#pragma unroll
+            for (int j = 0; j < CB; ++j) {
+                const float4 v = *reinterpret_cast<const float4*>(row + j * D + f);
+                acca[j] = fma2(make_float2(xa[f], xa[f + 1]), make_float2(v.x, v.y), acca[j]);
+                acca[j] = fma2(make_float2(xa[f + 2], xa[f + 3]), make_float2(v.z, v.w), acca[j]);
+                accb[j] = fma2(make_float2(xb[f], xb[f + 1]), make_float2(v.x, v.y), accb[j]);
+                accb[j] = fma2(make_float2(xb[f + 2], xb[f + 3]), make_float2(v.z, v.w), accb[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < CB; ++j) {
+            screen_track(fmaf(-2.0f, acca[j].x + acca[j].y, cn[c + j]), c + j, m1a, m2a, i1a);
+            screen_track(fmaf(-2.0f, accb[j].x + accb[j].y, cn[c + j]), c + j, m1b, m2b, i1b);
+        }
+    }
+    for (; c < k; ++c) {
+        const float* row = cs + (size_t)c * D;
+        float2 acca = make_float2(0.0f, 0.0f), accb = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int f = 0; f < D; f += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(row + f);
+            acca = fma2(make_float2(xa[f], xa[f + 1]), make_float2(v.x, v.y), acca);
+            acca = fma2(make_float2(xa[f + 2], xa[f + 3]), make_float2(v.z, v.w), acca);
+            accb = fma2(make_float2(xb[f], xb[f + 1]), make_float2(v.x, v.y), accb);
+            accb = fma2(make_float2(xb[f + 2], xb[f + 3]), make_float2(v.z, v.w), accb);
+        }
+        screen_track(fmaf(-2.0f, acca.x + acca.y, cn[c]), c, m1a, m2a, i1a);
+        screen_track(fmaf(-2.0f, accb.x + accb.y, cn[c]), c, m1b, m2b, i1b);
+    }
+    la = ((m1a < INFINITY) && (m2a - m1a > Ta) && (ra * ra < 0x1p120f)) ? i1a : label_rows_exact<D>(xa, cs, k);
+    lb = ((m1b < INFINITY) && (m2b - m1b > Tb) && (rb * rb < 0x1p120f)) ? i1b : label_rows_exact<D>(xb, cs, k);
 }
 
 // Prologue of the screen, run by every thread of a CTA after the centroid rows
