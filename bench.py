@@ -1103,7 +1103,7 @@ def main():
                          "at most 32 GiB)")
     ap.add_argument("--buffered-iterations", type=int, default=50, help="buffered workload: iterations per step")
     ap.add_argument("--no-simt-compare", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-spatial", action="store_true",
                     help="default workload: time the caller's point order only (no spatial sort, no box pruning)")
