@@ -1241,7 +1241,7 @@ def main():
         cfg = ckm.RunConfig(b"single_stage", b"feature_sum", b"unroll_vector", b"part_local", b"feature_sum",
                             local, 0, 0)
         info = ckm.RunInfo()
-        times = []
+        times, windows = [], []
         for _ in range(args.e2e_steps + 1):
             hostC.numpy()[:] = C0_host
             t0 = time.perf_counter()
@@ -1249,6 +1249,7 @@ def main():
                                                    hostC.data_ptr(), hostM.data_ptr(), hostL.data_ptr(),
                                                    ctypes.byref(info)), "ckm_kmeans_run_f32")
             times.append(time.perf_counter() - t0)
+            windows.append(info.total_time_ns / 1e6)
         # the median call: the host link and the host's memory are shared with
         # the box's other GPUs, and a call now and then takes 2-4x longer
         e2e_t = statistics.median(times[1:])
@@ -1259,6 +1260,7 @@ def main():
                "statistic": "median of %d calls after the first" % (len(times) - 1),
                "ms_per_step_mean": statistics.mean(times[1:]) * 1e3,
                "ms_per_call": [t * 1e3 for t in times],
+               "window_ms_per_call": windows,
                "first_call": "allocates the device buffers from the stream-ordered pool; not in ms_per_step",
                "total_time_window_ms": window_ms,
                "window_roofline_frac": bytes_per_point * n * iters_cfg / (window_ms / 1e3) / 1e9 / peak,
