@@ -19,6 +19,10 @@ an FP64 oracle.
   size-independent properties: both orders give the same masses and
   centroids, the masses sum to n, and a 2^20-point sample of the labels equals
   the oracle's.
+* The same workload end to end at its size through ckm_kmeans_run_f32 with
+  host buffers (50 iterations): masses against the label counts, centroids
+  against the FP64 means of the labels, a 2^20-point sample of the last
+  iteration's labels against the oracle.
 * Tensor-core Lloyd at its size (n = 2^24, d = 128, k = 1024): two
   iterations, a 16384-point sample of the labels against the oracle, masses
   against the label counts, centroids against the FP64 means of the labels.
@@ -241,3 +245,43 @@ def test_config4_full_size_lockstep(ckm, oracle, cuda):
         assert worst <= 1e-5, worst
     finally:
         b.close()
+
+
+def test_config2a_end_to_end_full_size(ckm, oracle, cuda):
+    """The HBM-scale workload end to end at its size through the C ABI with
+    host buffers: ckm_kmeans_run_f32 (single stage, 50 iterations, the
+    spatial order taken automatically) over n = 2^28, d = 4, k = 16.  The
+    returned masses equal the counts of the returned labels (which sum to n),
+    the returned centroids are within 1e-5 (normwise relative) of the FP64
+    means of the points under those labels, and on a 2^20-point sample the
+    labels equal the oracle's from the centroids the last iteration started
+    from (taken from a 49-iteration run; every mismatch adjudicated in FP64
+    against the derived near-tie bound)."""
+    import torch
+    n, d, k, iters = 1 << 28, 4, 16, 50
+    dP = _c2a(ckm, cuda, n)
+    P = dP.cpu().numpy()
+    C0 = dP.view(d, n)[:, :k].reshape(-1).cpu().numpy()
+    C, M, L, info = ckm.kmeans_run(P, d, k, iters, C0, pipeline="single_stage")
+    assert info.iterations == iters
+    dL = torch.from_numpy(L.view(np.int32)).to(cuda).long()
+    counts = torch.bincount(dL, minlength=k)
+    assert int(counts.sum().item()) == n
+    assert np.array_equal(M.astype(np.int64), counts.cpu().numpy())
+    sums = torch.zeros(k, d, dtype=torch.float64, device=cuda)
+    Pv = dP.view(d, n)
+    for s0 in range(0, n, 1 << 24):
+        sums.index_add_(0, dL[s0:s0 + (1 << 24)], Pv[:, s0:s0 + (1 << 24)].t().double())
+    full = (counts > 0).cpu().numpy()
+    means = (sums / counts.clamp(min=1).double()[:, None]).cpu().numpy()
+    got = C.reshape(d, k).T.astype(np.float64)
+    assert parity.rel_centroid_error(got[full], means[full]) <= 1e-5
+    del dL, sums
+    # the last iteration's labels on a sample, from a 49-iteration run's centroids
+    C49 = ckm.kmeans_run(P, d, k, iters - 1, C0, pipeline="single_stage")[0]
+    idx = np.sort(np.random.default_rng(5).choice(n, size=1 << 20, replace=False))
+    Xs = np.ascontiguousarray(P.reshape(d, n)[:, idx]).reshape(-1)
+    ref = oracle.label_f32(Xs, len(idx), d, k, C49)
+    got_l = L.view(np.uint32)[idx]
+    if np.any(got_l != ref):
+        parity.adjudicate(Xs, len(idx), d, k, got_l, ref, C49, C49, prev_slack_ulps=1)
