@@ -164,31 +164,6 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[3
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// The reference distance (kmeans_naive.cpp:52-57) from FP32 row-major copies
-// padded to 4 features: t = x_f - c_f, acc = fma(t, t, acc), f ascending.
-__device__ __forceinline__ float exact_distance(const float* __restrict__ x, const float* __restrict__ c, uint32_t d) {
-    float acc = 0.0f;
-    const float4* x4 = reinterpret_cast<const float4*>(x);
-    const float4* c4 = reinterpret_cast<const float4*>(c);
-    uint32_t f = 0;
-    for (; f + 4 <= d; f += 4) {
-        const float4 a = __ldg(x4 + f / 4), b = __ldg(c4 + f / 4);
-        float t = a.x - b.x;
-        acc = fmaf(t, t, acc);
-        t = a.y - b.y;
-        acc = fmaf(t, t, acc);
-        t = a.z - b.z;
-        acc = fmaf(t, t, acc);
-        t = a.w - b.w;
-        acc = fmaf(t, t, acc);
-    }
-    for (; f < d; ++f) {
-        const float t = __ldg(x + f) - __ldg(c + f);
-        acc = fmaf(t, t, acc);
-    }
-    return acc;
-}
-
 // --------------------------------------------------------------------------
 // Point preparation (once per point set)
 // --------------------------------------------------------------------------
